@@ -1,0 +1,384 @@
+#!/usr/bin/env python3
+"""Benchmark: FP64 CG cell-iterations/s of TeaLeaf's implicit solve at 8192^2 on GB300.
+
+Workload (synthetic config 5): 8192 x 8192 cells on the 10 x 10 domain, ambient state
+(density 100, energy 1e-4) + 16 seeded rectangles (density U[0.1,1], energy U[1,25]) +
+4 seeded circles (density 0.1, energy 25), reciprocal-density coefficient keyword,
+dt 0.004, tl_eps 1e-15, CG, FP64.  A step is one tea_leaf() time-step solve through the
+C ABI capped at --iters CG iterations (tl_max_iters): Kx/Ky/Di set-up, initial residual,
+--iters fused CG iterations, finalise.  At this size a full time step needs tens of
+thousands of iterations, so the cap keeps a step near 0.1 s; iterations are the work unit
+of the metric (cells x iterations / time), exactly as the reference's own grind figures.
+
+value  : device time (CUDA events on the solver stream) of the K timed steps, inputs
+         resident in HBM (every step reads ~14 fields of 0.54 GB: larger than L2).
+e2e    : the same steps through the C ABI with host buffers: density/energy uploaded from
+         pinned host memory, solve, energy downloaded, every step (host wall clock).
+roofline: the dominant kernel (fused p-update + matvec + p.w sweep) timed per launch with
+         CUDA events during the timed steps, against 48 B/cell of compulsory traffic.
+cpu_baseline: the CPU port (oracle/, OpenMP over all host cores) on a bounded sample of
+         the same workload (one time-step solve capped at --cpu-iters iterations).
+
+--impl reference times that CPU port alone as the reference arm.  Under torchrun (N>1)
+every rank runs an independent replica of the workload on its own GPU (the solve has no
+multi-GPU decomposition here), barrier + max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_CELL_MATVEC = 48  # r, p_old, Kx, Ky read; p, w written (8 B each)
+BYTES_PER_CELL_IT = 96      # whole FP64 CG iteration (12 streams)
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cells", type=int, default=8192)
+    ap.add_argument("--iters", type=int, default=100, help="CG iterations per step (tl_max_iters)")
+    ap.add_argument("--cpu-iters", type=int, default=5, help="CG iterations per CPU sample step")
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload(args):
+    from tealeaf_ref_gb300 import deck as dk
+
+    d = dk.config_deck(5, cells=args.cells)
+    d.max_iters = args.iters
+    return d
+
+
+def config_json(args, d):
+    return {
+        "workload": "TeaLeaf implicit diffusion, FP64 CG, %dx%d cells, 16 rectangles + 4 circles (seed 5), "
+                    "reciprocal-density keyword, dt 0.004, tl_eps 1e-15; step = one tea_leaf() solve capped at "
+                    "%d iterations" % (args.cells, args.cells, args.iters),
+        "cells": args.cells * args.cells,
+        "iterations_per_step": args.iters,
+        "solver": "cg",
+        "precision": "fp64",
+        "l2": "inputs larger than L2 (each field %.0f MB, ~14 fields touched per step)" % (
+            (args.cells + 2) * (args.cells + 18) * 8 / 1e6),
+    }
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            with open(p) as f:
+                j = json.load(f)
+            v = j.get("hbm_gbs") or j.get("hbm_GBps") or j.get("hbm")
+            if isinstance(v, dict):
+                v = v.get("burst") or v.get("value")
+            if v:
+                return float(v), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic():
+    p = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_port_steps(d, iters, steps, warmup, density=None, energy=None):
+    """Time the OpenMP CPU port (oracle) on one-step solves capped at `iters` iterations."""
+    from oracle import oracle
+
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    dd = d.replace(max_iters=iters)
+    c = oracle.Chunk(dd.x_cells, dd.y_cells, dd.halo_depth, dd.xmin, dd.ymin, dd.xmax, dd.ymax, dd.coefficient,
+                     dd.precond_id, dd.reflective_boundary, threaded=True)
+    if density is not None:
+        # state taken from the GPU generator (the CPU generator is slow at this size); halo
+        # cells get the ambient density, as generate_chunk gives them (boundary faces are
+        # zeroed afterwards, but their coefficient is still formed from it)
+        dens = c.array("density")
+        dens[...] = 100.0
+        c.interior("density")[...] = density
+        c.interior("energy1")[...] = energy
+    else:
+        c.generate(dd)
+        c.start_fields()
+    for _ in range(warmup):
+        c.tea_leaf(dd)
+    times, its = [], 0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        info = c.tea_leaf(dd)
+        times.append(time.perf_counter() - t0)
+        its += info.n_exit if info.n_exit <= iters else iters
+    return sum(times), its, cores
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    d = workload(args)
+    iters = args.cpu_iters
+    total, its, cores = cpu_port_steps(d, iters, args.steps, args.warmup)
+    cells = args.cells * args.cells
+    value = cells * its / total
+    out = {
+        "impl": "reference",
+        "metric": "CG cell-iterations/s (FP64, %d^2)" % args.cells,
+        "value": value,
+        "unit": "cell-iterations/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": dict(config_json(args, d), cpu_sample_iterations_per_step=iters),
+        "cpu_baseline": {"value": value, "unit": "cell-iterations/s", "cores": cores, "kind": "port",
+                         "sample": "%d timed one-step solves capped at %d CG iterations each, %dx%d cells, "
+                                   "OpenMP CPU port of the reference kernels" % (args.steps, iters, args.cells,
+                                                                                 args.cells)},
+        "e2e": {"value": value, "unit": "cell-iterations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+
+    import numpy as np
+
+    from tealeaf_ref_gb300 import native
+
+    native.set_device(local)
+    d = workload(args)
+    opts = native.opts_from_deck(d)
+    dt = d.initial_timestep
+    cells = args.cells * args.cells
+
+    chunk = native.Chunk.from_deck(d)
+    for _ in range(args.warmup):
+        chunk.tea_leaf(opts, dt)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident timed region ----
+    chunk.profile(True)
+    barrier()
+    infos = []
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            infos.append(chunk.tea_leaf(opts, dt))
+        wall = time.perf_counter() - t0
+    barrier()
+    dev_s = sum(i.solve_seconds for i in infos)
+    its = sum(min(i.n_exit, args.iters) for i in infos)
+    launches = sum(i.kernel_launches for i in infos)
+    mv_ms, mv_n = chunk.profile_read("cg_matvec")
+    up_ms, up_n = chunk.profile_read("cg_update")
+    chunk.profile(False)
+    t_max = max_over_ranks(dev_s)
+    value = world * cells * its / t_max
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        import torch
+
+        dens = torch.empty((args.cells, args.cells), dtype=torch.float64, pin_memory=True).numpy()
+        ener = torch.empty((args.cells, args.cells), dtype=torch.float64, pin_memory=True).numpy()
+        out = torch.empty((args.cells, args.cells), dtype=torch.float64, pin_memory=True).numpy()
+        dens[...] = chunk.download("density")
+        ener[...] = chunk.download("energy1")
+        chunk.upload_state(dens, ener)
+        chunk.tea_leaf(opts, dt)
+        barrier()
+        e_its = 0
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            chunk.upload_state(dens, ener)
+            info = chunk.tea_leaf(opts, dt)
+            e_its += min(info.n_exit, args.iters)
+            out[...] = chunk.download("energy1")
+        e_wall = time.perf_counter() - t0
+        barrier()
+        e_wall = max_over_ranks(e_wall)
+        e2e = {"value": world * cells * e_its / e_wall, "unit": "cell-iterations/s",
+               "h2d_bytes_per_step": 2 * cells * 8, "d2h_bytes_per_step": cells * 8,
+               "ms_per_step": 1e3 * e_wall / args.steps}
+        launches_e2e = None  # noqa: F841
+
+    peak, peak_kind = measured_peaks()
+    t_launch = mv_ms / mv_n * 1e-3 if mv_n else None
+    achieved = BYTES_PER_CELL_MATVEC * cells / t_launch / 1e9 if t_launch else None
+    traffic = ncu_traffic()
+    per_launch_traffic = None
+    if traffic and traffic.get("cells"):
+        per_launch_traffic = traffic["bytes_per_cell"] * cells
+    roofline = {
+        "bound": "hbm",
+        "kernel": "k_fused_cg_w (p = r + beta p, w = A p, p.w)",
+        "achieved": achieved,
+        "peak": peak,
+        "unit": "GB/s",
+        "frac": achieved / peak if achieved else None,
+        "peak_source": peak_kind,
+        "traffic": per_launch_traffic,
+        "algorithmic_bytes_per_cell": BYTES_PER_CELL_MATVEC,
+        "launch_ms": mv_ms / mv_n if mv_n else None,
+        "launches": mv_n,
+        "update_kernel_launch_ms": up_ms / up_n if up_n else None,
+        "iteration_gbs_at_96B": BYTES_PER_CELL_IT * cells * its / dev_s / 1e9 if dev_s else None,
+        "note": "FP64 issue rate (measured 0.60 T DFMA/s) bounds the sweep before HBM does",
+    }
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            total, cits, cores = cpu_port_steps(d, args.cpu_iters, args.cpu_steps, 1, dens if e2e else None,
+                                                ener if e2e else None)
+            cpu = {"value": cells * cits / total, "unit": "cell-iterations/s", "cores": cores, "kind": "port",
+                   "sample": "%d one-step solves capped at %d CG iterations, %dx%d cells, OpenMP CPU port of the "
+                             "reference kernels (oracle/)" % (args.cpu_steps, args.cpu_iters, args.cells,
+                                                              args.cells)}
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "cell-iterations/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": "failed: %s" % e}
+
+    if rank == 0:
+        out = {
+            "metric": "CG cell-iterations/s (FP64, %d^2)" % args.cells,
+            "value": value,
+            "unit": "cell-iterations/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_max / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic",
+            "config": dict(config_json(args, d), parallelism="replicas" if world > 1 else "single"),
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "wall_s_timed": wall,
+        }
+        print(json.dumps(out), flush=True)
+    chunk.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,952 @@
+// tl_api.cu -- the C ABI (include/tealeaf_gb300.h): context, host<->device copies, the
+// per-kernel drop-in entry points and tl_tea_leaf(), a C++ restatement of the control flow
+// of tea_leaf() (tea_solve.f90:37-503) over the GPU kernels.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/tealeaf_gb300.h"
+#include "tl_kernels.cuh"
+
+using namespace tl;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* msg) {
+  g_err = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char* where) {
+  g_err = std::string(where) + ": " + cudaGetErrorString(e);
+  return TL_ERR_CUDA;
+}
+
+#define CK(call)                                   \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+// field order inside the slab
+enum Slot {
+  S_DENSITY, S_ENERGY1, S_U, S_U0, S_R, S_W, S_P, S_P2, S_KX, S_KY, S_CX, S_CY, S_DI, S_Z, S_MI, S_SD, S_SD1,
+  S_UTEMP, S_RTEMP, S_RSTORE, S_CP, S_BFP, S_U1, S_JINV, S_COUNT
+};
+
+}  // namespace
+
+struct tl_ctx {
+  int device = 0;
+  Layout L{};
+  Geometry g{};
+  int halo_depth = 1;
+  cudaStream_t stream = nullptr;
+  char* slab = nullptr;
+  size_t slab_bytes = 0;
+  size_t field_stride = 0;  // bytes between fields in the slab
+  Fields f{};
+  double* partials = nullptr;
+  unsigned* counter = nullptr;
+  LoopState* st = nullptr;
+  LoopState* st_host = nullptr;  // pinned mirror
+  double* hist_a = nullptr;
+  double* hist_b = nullptr;
+  int hist_cap = 0;
+  double* ch_a = nullptr;
+  double* ch_b = nullptr;
+  int ch_cap = 0;
+  double* states_dev = nullptr;
+  int states_cap = 0;
+  double** halo_list = nullptr;  // device array of field pointers for halo updates
+  // reference SAVE variables (tea_solve.f90:55,58)
+  int first = 1;
+  double eigmin = 0, eigmax = 0, theta = 0, cn = 0;
+  bool have_coefs = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // per-launch timers of the fused loop kernels (tl_profile)
+  static constexpr int BATCH = 16;
+  bool prof = false;
+  cudaEvent_t pev[3 * BATCH] = {};
+  double prof_ms[TL_NUM_KERNEL_TIMERS] = {};
+  long long prof_n[TL_NUM_KERNEL_TIMERS] = {};
+  long long nlaunch = 0;  // kernels launched by the current tl_tea_leaf call
+
+  double* slot(int s) const { return reinterpret_cast<double*>(slab + (size_t)s * field_stride); }
+  Reduce rd() const { return Reduce{partials, counter, st, hist_a, hist_b, ch_a, ch_b}; }
+  LoopArgs loop() const { return LoopArgs{f, L, rd(), g.precond, g.reflective, g.ry}; }
+};
+
+namespace {
+
+double* field_ptr(tl_ctx* c, int id) {
+  switch (id) {
+    case TL_FIELD_DENSITY: return c->f.density;
+    case TL_FIELD_ENERGY0:
+    case TL_FIELD_ENERGY1: return c->f.energy1;
+    case TL_FIELD_U: return c->f.u;
+    case TL_FIELD_P: return c->f.p;
+    case TL_FIELD_SD: return c->f.sd;
+    case TL_FIELD_R: return c->f.r;
+    case TL_FIELD_Z: return c->f.z;
+    case TL_FIELD_KX: return c->f.kx;
+    case TL_FIELD_KY: return c->f.ky;
+    case TL_FIELD_DI: return c->f.di;
+    case TL_FIELD_U0: return c->f.u0;
+    case TL_FIELD_W: return c->f.w;
+    case TL_FIELD_MI: return c->f.mi;
+    case TL_FIELD_UTEMP: return c->f.utemp;
+    case TL_FIELD_RTEMP: return c->f.rtemp;
+    case TL_FIELD_R_STORE: return c->f.r_store;
+    default: return nullptr;
+  }
+}
+
+// update_halo field binding (update_halo.f90:64-80): FIELD_R is vector_rtemp there.
+double* halo_field_ptr(tl_ctx* c, int id) {
+  if (id == TL_FIELD_R) return c->f.rtemp;
+  if (id == TL_FIELD_ENERGY0) return nullptr;  // energy0 is not held on the device
+  return field_ptr(c, id);
+}
+
+int sync_state(tl_ctx* c) {
+  CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(LoopState), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int push_state(tl_ctx* c) {
+  CK(cudaMemcpyAsync(c->st, c->st_host, sizeof(LoopState), cudaMemcpyHostToDevice, c->stream));
+  return TL_OK;
+}
+
+int reduce_result(tl_ctx* c, double* out, int lanes = 1) {
+  int rc = sync_state(c);
+  if (rc) return rc;
+  for (int i = 0; i < lanes; ++i) out[i] = c->st_host->red[i];
+  return TL_OK;
+}
+
+int check_launch(const char* where) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, where);
+  return TL_OK;
+}
+
+int ensure_hist(tl_ctx* c, int n) {
+  if (n <= c->hist_cap) return TL_OK;
+  if (c->hist_a) cudaFree(c->hist_a);
+  if (c->hist_b) cudaFree(c->hist_b);
+  c->hist_a = c->hist_b = nullptr;
+  CK(cudaMalloc(&c->hist_a, sizeof(double) * n));
+  CK(cudaMalloc(&c->hist_b, sizeof(double) * n));
+  c->hist_cap = n;
+  return TL_OK;
+}
+
+int ensure_ch(tl_ctx* c, int n) {
+  if (n <= c->ch_cap) return TL_OK;
+  if (c->ch_a) cudaFree(c->ch_a);
+  if (c->ch_b) cudaFree(c->ch_b);
+  c->ch_a = c->ch_b = nullptr;
+  CK(cudaMalloc(&c->ch_a, sizeof(double) * n));
+  CK(cudaMalloc(&c->ch_b, sizeof(double) * n));
+  c->ch_cap = n;
+  return TL_OK;
+}
+
+int do_halo(tl_ctx* c, int mask, int depth) {
+  (void)depth;  // a single chunk reads only the first halo layer
+  if (!c->g.reflective) return TL_OK;
+  double* ptrs[TL_FIELD_DI + 1];
+  int n = 0;
+  for (int id = 1; id <= TL_FIELD_DI; ++id)
+    if (mask & (1 << id)) {
+      double* p = halo_field_ptr(c, id);
+      if (p) ptrs[n++] = p;
+    }
+  if (!n) return TL_OK;
+  CK(cudaMemcpyAsync(c->halo_list, ptrs, sizeof(double*) * n, cudaMemcpyHostToDevice, c->stream));
+  launch_update_halo(c->halo_list, n, c->L, c->stream);
+  return check_launch("update_halo");
+}
+
+constexpr int M(int id) { return 1 << id; }
+
+// ---------------------------------------------------------------------------
+// Host scalar math: eigenvalues of the Lanczos tridiagonal built from the CG
+// coefficients (tea_leaf_cheby.f90:142-176) and the Chebyshev coefficients (:178-205).
+// Extreme eigenvalues by bisection on the Sturm sequence of T - x I (Golub & Van Loan,
+// Matrix Computations, 4th ed., sec. 8.4.1).
+// ---------------------------------------------------------------------------
+int sturm_below(const std::vector<double>& d, const std::vector<double>& e2, double x) {
+  const double tiny = 1e-300;
+  int neg = 0;
+  double q = 1.0;
+  for (size_t i = 0; i < d.size(); ++i) {
+    q = d[i] - x - (i ? e2[i - 1] / q : 0.0);
+    if (q == 0.0) q = -tiny;
+    if (q < 0.0) ++neg;
+  }
+  return neg;
+}
+
+double bisect_eigen(const std::vector<double>& d, const std::vector<double>& e2, int which, double lo, double hi) {
+  for (int it = 0; it < 4000; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) break;
+    if (sturm_below(d, e2, mid) > which)
+      hi = mid;
+    else
+      lo = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+int calc_eigenvalues(const std::vector<double>& alphas, const std::vector<double>& betas, int nsteps, double* eigmin,
+                     double* eigmax) {
+  // alphas[i], betas[i] hold cg_alphas(i+1), cg_betas(i+1)
+  if (nsteps <= 0) return 1;
+  std::vector<double> d(nsteps), off(nsteps > 1 ? nsteps - 1 : 0), e2(off.size());
+  for (int n = 0; n < nsteps; ++n) {
+    d[n] = 1.0 / alphas[n];
+    if (n > 0) d[n] = d[n] + betas[n - 1] / alphas[n - 1];
+    if (n < nsteps - 1) off[n] = std::sqrt(betas[n]) / alphas[n];
+  }
+  double lo = d[0], hi = d[0];
+  for (int i = 0; i < nsteps; ++i) {
+    const double rad = (i > 0 ? std::fabs(off[i - 1]) : 0.0) + (i < nsteps - 1 ? std::fabs(off[i]) : 0.0);
+    lo = std::fmin(lo, d[i] - rad);
+    hi = std::fmax(hi, d[i] + rad);
+  }
+  const double pad = 4.0 * 2.220446049250313e-16 * std::fmax(std::fabs(lo), std::fabs(hi)) + 1e-300;
+  lo -= pad;
+  hi += pad;
+  for (size_t i = 0; i < off.size(); ++i) e2[i] = off[i] * off[i];
+  *eigmin = bisect_eigen(d, e2, 0, lo, hi);
+  *eigmax = bisect_eigen(d, e2, nsteps - 1, lo, hi);
+  if (!(std::isfinite(*eigmin) && std::isfinite(*eigmax))) return 1;
+  if (*eigmin < 0.0 || *eigmax < 0.0) return 1;
+  return 0;
+}
+
+void calc_ch_coefs(std::vector<double>& a, std::vector<double>& b, double eigmin, double eigmax, double* theta, int n) {
+  *theta = (eigmax + eigmin) / 2;
+  const double delta = (eigmax - eigmin) / 2;
+  const double sigma = *theta / delta;
+  double rho_old = 1.0 / sigma;
+  a.assign(n + 1, 0.0);
+  b.assign(n + 1, 0.0);
+  for (int i = 1; i <= n; ++i) {
+    const double rho_new = 1.0 / (2.0 * sigma - rho_old);
+    a[i] = rho_new * rho_old;
+    b[i] = 2.0 * rho_new / delta;
+    rho_old = rho_new;
+  }
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* tl_last_error(void) { return g_err.c_str(); }
+
+int tl_set_device(int device) {
+  int n = 0;
+  CK(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) return fail(TL_ERR_ARG, "tl_set_device: no such device");
+  CK(cudaSetDevice(device));
+  return TL_OK;
+}
+
+int tl_create(int x_cells, int y_cells, int halo_depth, int coefficient, int preconditioner, int reflective_boundary,
+              double dx, double dy, tl_ctx** out) {
+  if (!out) return fail(TL_ERR_ARG, "tl_create: out is null");
+  *out = nullptr;
+  if (x_cells < 1 || y_cells < 1 || x_cells > 65536 || y_cells > 65536)
+    return fail(TL_ERR_ARG, "tl_create: x_cells and y_cells must be in 1..65536");
+  if (halo_depth < 1) return fail(TL_ERR_ARG, "tl_create: Invalid halo exchange depth specified");
+  if (coefficient != TL_CONDUCTIVITY && coefficient != TL_RECIP_CONDUCTIVITY)
+    return fail(TL_ERR_ARG, "tl_create: unknown coefficient option");
+  if (preconditioner < TL_PREC_NONE || preconditioner > TL_PREC_JAC_BLOCK)
+    return fail(TL_ERR_ARG, "tl_create: Invalid preconditioner type specified");
+  if (halo_depth > 1 && preconditioner == TL_PREC_JAC_BLOCK)
+    return fail(TL_ERR_ARG, "tl_create: Unable to use nonstandard halo depth with block jacobi preconditioner");
+  if (!(dx > 0.0) || !(dy > 0.0)) return fail(TL_ERR_ARG, "tl_create: dx and dy must be positive");
+
+  tl_ctx* c = new tl_ctx();
+  cudaGetDevice(&c->device);
+  c->halo_depth = halo_depth;
+  c->L.nx = x_cells;
+  c->L.ny = y_cells;
+  c->L.ld = ((XOFF + x_cells + 2 + 15) / 16) * 16;
+  c->g.dx = dx;
+  c->g.dy = dy;
+  c->g.coefficient = coefficient;
+  c->g.precond = preconditioner;
+  c->g.reflective = reflective_boundary ? 1 : 0;
+
+  const size_t field_bytes = ((size_t)c->L.elems() * sizeof(double) + 4 * 256 + 255) / 256 * 256;
+  c->field_stride = field_bytes;
+  c->slab_bytes = field_bytes * S_COUNT;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&c->slab, c->slab_bytes);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->slab, 0, c->slab_bytes, c->stream);
+  if (e == cudaSuccess) e = cudaMalloc(&c->partials, sizeof(double) * 4 * MAX_REDUCE_BLOCKS);
+  if (e == cudaSuccess) e = cudaMalloc(&c->counter, 256);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->counter, 0, 256, c->stream);
+  if (e == cudaSuccess) e = cudaMalloc(&c->st, sizeof(LoopState));
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->st, 0, sizeof(LoopState), c->stream);
+  if (e == cudaSuccess) e = cudaMallocHost(&c->st_host, sizeof(LoopState));
+  if (e == cudaSuccess) e = cudaMalloc(&c->halo_list, sizeof(double*) * 16);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  for (int i = 0; i < 3 * tl_ctx::BATCH && e == cudaSuccess; ++i) e = cudaEventCreate(&c->pev[i]);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    int rc = (e == cudaErrorMemoryAllocation) ? TL_ERR_ALLOC : TL_ERR_CUDA;
+    g_err = std::string("tl_create: ") + cudaGetErrorString(e);
+    cudaGetLastError();
+    tl_destroy(c);
+    return rc;
+  }
+  memset(c->st_host, 0, sizeof(LoopState));
+  Fields& f = c->f;
+  f.density = c->slot(S_DENSITY);
+  f.energy1 = c->slot(S_ENERGY1);
+  f.u = c->slot(S_U);
+  f.u0 = c->slot(S_U0);
+  f.r = c->slot(S_R);
+  f.w = c->slot(S_W);
+  f.p = c->slot(S_P);
+  f.p2 = c->slot(S_P2);
+  f.kx = c->slot(S_KX);
+  f.ky = c->slot(S_KY);
+  f.cx = c->slot(S_CX);
+  f.cy = c->slot(S_CY);
+  f.di = c->slot(S_DI);
+  f.z = c->slot(S_Z);
+  f.mi = c->slot(S_MI);
+  f.sd = c->slot(S_SD);
+  f.sd1 = c->slot(S_SD1);
+  f.utemp = c->slot(S_UTEMP);
+  f.rtemp = c->slot(S_RTEMP);
+  f.r_store = c->slot(S_RSTORE);
+  f.cp = c->slot(S_CP);
+  f.bfp = c->slot(S_BFP);
+  f.u1 = c->slot(S_U1);
+  f.jinv = c->slot(S_JINV);
+  *out = c;
+  return TL_OK;
+}
+
+int tl_destroy(tl_ctx* c) {
+  if (!c) return fail(TL_ERR_ARG, "tl_destroy: null context");
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  cudaFree(c->slab);
+  cudaFree(c->partials);
+  cudaFree(c->counter);
+  cudaFree(c->st);
+  if (c->st_host) cudaFreeHost(c->st_host);
+  cudaFree(c->hist_a);
+  cudaFree(c->hist_b);
+  cudaFree(c->ch_a);
+  cudaFree(c->ch_b);
+  cudaFree(c->states_dev);
+  cudaFree(c->halo_list);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  for (int i = 0; i < 3 * tl_ctx::BATCH; ++i)
+    if (c->pev[i]) cudaEventDestroy(c->pev[i]);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return TL_OK;
+}
+
+int tl_device_bytes(const tl_ctx* c, unsigned long long* bytes) {
+  if (!c || !bytes) return fail(TL_ERR_ARG, "tl_device_bytes: null argument");
+  *bytes = c->slab_bytes + sizeof(double) * 4 * MAX_REDUCE_BLOCKS + 256 + sizeof(LoopState) +
+           sizeof(double) * 2 * ((size_t)c->hist_cap + c->ch_cap);
+  return TL_OK;
+}
+
+int tl_upload_field(tl_ctx* c, int field, const double* host, int ld) {
+  if (!c || !host) return fail(TL_ERR_ARG, "tl_upload_field: null argument");
+  double* d = field_ptr(c, field);
+  if (!d) return fail(TL_ERR_ARG, "tl_upload_field: unknown field id");
+  if (ld < c->L.nx) return fail(TL_ERR_ARG, "tl_upload_field: ld < x_cells");
+  CK(cudaMemcpy2DAsync(d + c->L.at(1, 1), sizeof(double) * c->L.ld, host, sizeof(double) * ld,
+                       sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_download_field(tl_ctx* c, int field, double* host, int ld) {
+  if (!c || !host) return fail(TL_ERR_ARG, "tl_download_field: null argument");
+  double* d = field_ptr(c, field);
+  if (!d) return fail(TL_ERR_ARG, "tl_download_field: unknown field id");
+  if (ld < c->L.nx) return fail(TL_ERR_ARG, "tl_download_field: ld < x_cells");
+  CK(cudaMemcpy2DAsync(host, sizeof(double) * ld, d + c->L.at(1, 1), sizeof(double) * c->L.ld,
+                       sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_upload_state(tl_ctx* c, const double* density, const double* energy1, int ld) {
+  if (!c || !density || !energy1) return fail(TL_ERR_ARG, "tl_upload_state: null argument");
+  if (ld < c->L.nx) return fail(TL_ERR_ARG, "tl_upload_state: ld < x_cells");
+  // Work fields need no clearing: every solve initialises what it reads, and halo cells stay
+  // finite (zero from tl_create, or the generator's / reflective copies).
+  CK(cudaMemcpy2DAsync(c->f.density + c->L.at(1, 1), sizeof(double) * c->L.ld, density, sizeof(double) * ld,
+                       sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpy2DAsync(c->f.energy1 + c->L.at(1, 1), sizeof(double) * c->L.ld, energy1, sizeof(double) * ld,
+                       sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyHostToDevice, c->stream));
+  if (c->g.reflective) {
+    int rc = do_halo(c, M(TL_FIELD_DENSITY) | M(TL_FIELD_ENERGY1), c->halo_depth);
+    if (rc) return rc;
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_generate_chunk(tl_ctx* c, int nstates, const double* density, const double* energy, const double* xmin,
+                      const double* xmax, const double* ymin, const double* ymax, const double* radius,
+                      const int* geometry, double domain_xmin, double domain_ymin) {
+  if (!c || nstates < 1 || !density || !energy || !xmin || !xmax || !ymin || !ymax || !radius || !geometry)
+    return fail(TL_ERR_ARG, "tl_generate_chunk: invalid argument");
+  std::vector<double> st(8 * (size_t)nstates);
+  for (int s = 0; s < nstates; ++s) {
+    // read_input.f90:352-359: states 2.. are nudged by a hundredth of a cell
+    const double nx = s ? c->g.dx / 100.0 : 0.0, ny = s ? c->g.dy / 100.0 : 0.0;
+    st[8 * s + 0] = density[s];
+    st[8 * s + 1] = energy[s];
+    st[8 * s + 2] = xmin[s] + nx;
+    st[8 * s + 3] = xmax[s] - nx;
+    st[8 * s + 4] = ymin[s] + ny;
+    st[8 * s + 5] = ymax[s] - ny;
+    st[8 * s + 6] = radius[s];
+    st[8 * s + 7] = (double)geometry[s];
+  }
+  if (nstates > c->states_cap) {
+    cudaFree(c->states_dev);
+    c->states_dev = nullptr;
+    CK(cudaMalloc(&c->states_dev, st.size() * sizeof(double)));
+    c->states_cap = nstates;
+  }
+  CK(cudaMemsetAsync(c->slab, 0, c->slab_bytes, c->stream));
+  CK(cudaMemcpyAsync(c->states_dev, st.data(), st.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  launch_generate(c->f, c->L, nstates, c->states_dev, domain_xmin, domain_ymin, c->g.dx, c->g.dy, c->stream);
+  int rc = check_launch("generate_chunk");
+  if (rc) return rc;
+  // start.f90:113-118: prime density / energy halos (reflective only)
+  rc = do_halo(c, M(TL_FIELD_DENSITY) | M(TL_FIELD_ENERGY1), c->halo_depth);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));  // states_dev is host-synchronous input
+  return TL_OK;
+}
+
+int tl_field_summary(tl_ctx* c, double* vol, double* mass, double* ie, double* temp) {
+  if (!c || !vol || !mass || !ie || !temp) return fail(TL_ERR_ARG, "tl_field_summary: null argument");
+  launch_field_summary(c->f, c->L, c->g.dx * c->g.dy, c->rd(), c->stream);
+  int rc = check_launch("field_summary");
+  if (rc) return rc;
+  double out[4];
+  rc = reduce_result(c, out, 4);
+  if (rc) return rc;
+  *vol = out[0];
+  *mass = out[1];
+  *ie = out[2];
+  *temp = out[3];
+  return TL_OK;
+}
+
+// ---- per-kernel entry points ---------------------------------------------
+
+int tl_common_init(tl_ctx* c, double dt) {
+  if (!c) return fail(TL_ERR_ARG, "tl_common_init: null context");
+  c->g.rx = dt / (c->g.dx * c->g.dx);
+  c->g.ry = dt / (c->g.dy * c->g.dy);
+  launch_init_faces(c->f, c->L, c->g, c->stream);
+  launch_init_cells(c->f, c->L, c->g, true, c->stream);
+  int rc = check_launch("common_init");
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_calc_residual(tl_ctx* c) {
+  if (!c) return fail(TL_ERR_ARG, "tl_calc_residual: null context");
+  launch_residual(c->f, c->L, nullptr, RED_STORE, c->stream);
+  int rc = check_launch("calc_residual");
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_calc_2norm(tl_ctx* c, int norm_array, double* norm) {
+  if (!c || !norm) return fail(TL_ERR_ARG, "tl_calc_2norm: null argument");
+  if (norm_array != 0 && norm_array != 1) return fail(TL_ERR_ARG, "tl_calc_2norm: Invalid value for norm_array");
+  launch_norm2(norm_array == 0 ? c->f.u0 : c->f.r, c->L, c->rd(), RED_STORE, c->stream);
+  int rc = check_launch("calc_2norm");
+  if (rc) return rc;
+  return reduce_result(c, norm);
+}
+
+int tl_finalise(tl_ctx* c) {
+  if (!c) return fail(TL_ERR_ARG, "tl_finalise: null context");
+  launch_finalise(c->f, c->L, c->stream);
+  int rc = check_launch("finalise");
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_cg_init(tl_ctx* c, double* rro) {
+  if (!c || !rro) return fail(TL_ERR_ARG, "tl_cg_init: null argument");
+  launch_cg_init(c->f, c->L, c->g, c->rd(), RED_STORE, c->stream);
+  int rc = check_launch("cg_init");
+  if (rc) return rc;
+  return reduce_result(c, rro);
+}
+
+int tl_cg_calc_w(tl_ctx* c, double* pw) {
+  if (!c || !pw) return fail(TL_ERR_ARG, "tl_cg_calc_w: null argument");
+  launch_cg_calc_w(c->f, c->L, c->rd(), c->stream);
+  int rc = check_launch("cg_calc_w");
+  if (rc) return rc;
+  return reduce_result(c, pw);
+}
+
+int tl_cg_calc_ur(tl_ctx* c, double alpha, double* rrn) {
+  if (!c || !rrn) return fail(TL_ERR_ARG, "tl_cg_calc_ur: null argument");
+  launch_cg_calc_ur(c->f, c->L, c->g, alpha, c->rd(), c->stream);
+  int rc = check_launch("cg_calc_ur");
+  if (rc) return rc;
+  return reduce_result(c, rrn);
+}
+
+int tl_cg_calc_p(tl_ctx* c, double beta, int ppcg_active) {
+  if (!c) return fail(TL_ERR_ARG, "tl_cg_calc_p: null context");
+  launch_cg_calc_p(c->f, c->L, beta, c->g.precond != TL_PREC_NONE || ppcg_active, c->stream);
+  int rc = check_launch("cg_calc_p");
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_cheby_init(tl_ctx* c, double theta) {
+  if (!c) return fail(TL_ERR_ARG, "tl_cheby_init: null context");
+  launch_cheby_init(c->f, c->L, c->g, theta, c->stream);
+  int rc = check_launch("cheby_init");
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_cheby_iterate(tl_ctx* c, double a, double b) {
+  if (!c) return fail(TL_ERR_ARG, "tl_cheby_iterate: null context");
+  launch_cheby_iterate(c->f, c->L, c->g, a, b, c->stream);
+  int rc = check_launch("cheby_iterate");
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_ppcg_init_sd(tl_ctx* c, double theta) {
+  if (!c) return fail(TL_ERR_ARG, "tl_ppcg_init_sd: null context");
+  launch_ppcg_init_sd(c->f, c->L, c->g, theta, c->stream);
+  int rc = check_launch("ppcg_init_sd");
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_ppcg_init(tl_ctx* c, int step, int ppcg_active, double* rro) {
+  if (!c || !rro) return fail(TL_ERR_ARG, "tl_ppcg_init: null argument");
+  if (step < 1 || step > 3) return fail(TL_ERR_ARG, "tl_ppcg_init: step must be 1, 2 or 3");
+  launch_ppcg_init(c->f, c->L, c->g, step, ppcg_active != 0, c->rd(), RED_STORE, c->stream);
+  int rc = check_launch("ppcg_init");
+  if (rc) return rc;
+  if (step == 2) {
+    CK(cudaStreamSynchronize(c->stream));
+    *rro = 0.0;
+    return TL_OK;
+  }
+  return reduce_result(c, rro);
+}
+
+int tl_ppcg_inner(tl_ctx* c, double a, double b) {
+  if (!c) return fail(TL_ERR_ARG, "tl_ppcg_inner: null context");
+  launch_ppcg_inner(c->f, c->L, c->g, a, b, c->stream);
+  int rc = check_launch("ppcg_inner");
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_ppcg_calc_zrnorm(tl_ctx* c, int ppcg_active, double* rrn) {
+  if (!c || !rrn) return fail(TL_ERR_ARG, "tl_ppcg_calc_zrnorm: null argument");
+  const double* a = (c->g.precond != TL_PREC_NONE || ppcg_active) ? c->f.z : c->f.r;
+  launch_dot(a, c->f.r, nullptr, c->L, c->rd(), RED_STORE, c->stream);
+  int rc = check_launch("ppcg_calc_zrnorm");
+  if (rc) return rc;
+  return reduce_result(c, rrn);
+}
+
+int tl_ppcg_update_z(tl_ctx* c) {
+  if (!c) return fail(TL_ERR_ARG, "tl_ppcg_update_z: null context");
+  launch_copy_interior(c->f.z, c->f.utemp, c->L, c->stream);
+  int rc = check_launch("ppcg_update_z");
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_ppcg_store_r(tl_ctx* c) {
+  if (!c) return fail(TL_ERR_ARG, "tl_ppcg_store_r: null context");
+  launch_copy_interior(c->f.r_store, c->f.r, c->L, c->stream);
+  int rc = check_launch("ppcg_store_r");
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_ppcg_calc_rrn(tl_ctx* c, double* rrn) {
+  if (!c || !rrn) return fail(TL_ERR_ARG, "tl_ppcg_calc_rrn: null argument");
+  launch_dot(c->f.z, c->f.r, c->f.r_store, c->L, c->rd(), RED_STORE, c->stream);
+  int rc = check_launch("ppcg_calc_rrn");
+  if (rc) return rc;
+  return reduce_result(c, rrn);
+}
+
+int tl_jacobi_solve(tl_ctx* c, double* error) {
+  if (!c || !error) return fail(TL_ERR_ARG, "tl_jacobi_solve: null argument");
+  launch_jacobi_denominator(c->f, c->L, c->g, c->stream);
+  launch_jacobi(c->f, c->L, c->rd(), c->stream);
+  int rc = check_launch("jacobi_solve");
+  if (rc) return rc;
+  return reduce_result(c, error);
+}
+
+int tl_update_halo(tl_ctx* c, int field_mask, int depth) {
+  if (!c) return fail(TL_ERR_ARG, "tl_update_halo: null context");
+  if (depth < 1) return fail(TL_ERR_ARG, "tl_update_halo: depth must be >= 1");
+  int rc = do_halo(c, field_mask, depth);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_reset_eigen(tl_ctx* c) {
+  if (!c) return fail(TL_ERR_ARG, "tl_reset_eigen: null context");
+  c->first = 1;
+  c->have_coefs = false;
+  return TL_OK;
+}
+
+int tl_profile(tl_ctx* c, int enable) {
+  if (!c) return fail(TL_ERR_ARG, "tl_profile: null context");
+  c->prof = enable != 0;
+  if (c->prof)
+    for (int i = 0; i < TL_NUM_KERNEL_TIMERS; ++i) {
+      c->prof_ms[i] = 0.0;
+      c->prof_n[i] = 0;
+    }
+  return TL_OK;
+}
+
+int tl_profile_read(tl_ctx* c, int kernel_id, double* total_ms, long long* launches) {
+  if (!c || !total_ms || !launches) return fail(TL_ERR_ARG, "tl_profile_read: null argument");
+  if (kernel_id < 0 || kernel_id >= TL_NUM_KERNEL_TIMERS) return fail(TL_ERR_ARG, "tl_profile_read: bad kernel id");
+  *total_ms = c->prof_ms[kernel_id];
+  *launches = c->prof_n[kernel_id];
+  return TL_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// tl_tea_leaf
+// ===========================================================================
+namespace {
+
+struct Solver {
+  tl_ctx* c;
+  const tl_solve_opts* o;
+  int use_cg, use_cheby, use_ppcg, use_jacobi;
+  std::vector<double> ch_a, ch_b;
+
+  // reductions through the per-kernel path, result on the host
+  int norm(const double* a, double* out) {
+    launch_norm2(a, c->L, c->rd(), RED_STORE, c->stream);
+    int rc = check_launch("norm2");
+    if (rc) return rc;
+    return reduce_result(c, out);
+  }
+
+  int run_ppcg_inner_steps(int inner_steps) {
+    // tea_leaf_ppcg.f90:211-431 on one chunk (every face external: bounds = interior)
+    if (inner_steps < 0) return TL_OK;
+    launch_ppcg_init_sd(c->f, c->L, c->g, c->theta, c->stream);
+    const int h = c->halo_depth;
+    int rc;
+    for (int cur = 1; cur <= inner_steps; cur += h) {
+      if ((rc = do_halo(c, M(TL_FIELD_SD) | M(TL_FIELD_R), h))) return rc;
+      for (int be = h - 1; be >= 0; --be) {
+        const int step = cur + h - 1 - be;
+        launch_ppcg_inner(c->f, c->L, c->g, ch_a[step], ch_b[step], c->stream);
+        if (c->g.reflective && (rc = do_halo(c, M(TL_FIELD_SD), 1))) return rc;
+        if (step == inner_steps) break;
+      }
+    }
+    launch_copy_interior(c->f.z, c->f.utemp, c->L, c->stream);
+    return check_launch("ppcg_inner_steps");
+  }
+};
+
+}  // namespace
+
+extern "C" int tl_tea_leaf(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info) {
+  if (!c || !o || !info) return fail(TL_ERR_ARG, "tl_tea_leaf: null argument");
+  if (o->solver < TL_SOLVER_JACOBI || o->solver > TL_SOLVER_PPCG) return fail(TL_ERR_ARG, "tl_tea_leaf: bad solver");
+  if (o->max_iters < 1) return fail(TL_ERR_ARG, "tl_tea_leaf: max_iters must be >= 1");
+  memset(info, 0, sizeof(*info));
+  Solver S{c, o, o->solver == TL_SOLVER_CG, o->solver == TL_SOLVER_CHEBY, o->solver == TL_SOLVER_PPCG,
+           o->solver == TL_SOLVER_JACOBI, {}, {}};
+  int rc;
+  const int max_iters = o->max_iters;
+  if ((rc = ensure_hist(c, max_iters + 2))) return rc;
+  const int inner = o->ppcg_inner_steps;
+  if ((rc = ensure_ch(c, std::max(max_iters + 2, inner + 2)))) return rc;
+  const long long launches0 = launch_counter();
+  CK(cudaEventRecord(c->ev0, c->stream));
+
+  // ---- INIT (tea_solve.f90:86-146) ----
+  if ((rc = do_halo(c, M(TL_FIELD_ENERGY1) | M(TL_FIELD_DENSITY), c->halo_depth))) return rc;
+  c->g.rx = dt / (c->g.dx * c->g.dx);
+  c->g.ry = dt / (c->g.dy * c->g.dy);
+  launch_init_faces(c->f, c->L, c->g, c->stream);
+  launch_init_cells(c->f, c->L, c->g, false, c->stream);
+  if ((rc = do_halo(c, M(TL_FIELD_U), 1))) return rc;
+  LoopState& H = *c->st_host;
+  memset(&H, 0, sizeof(H));
+  H.eps = o->eps;
+  H.epslim = o->ch_cg_epslim;
+  H.presteps = o->ch_cg_presteps;
+  H.max_iters = max_iters;
+  H.first = c->first;
+  H.use_ppcg = S.use_ppcg;
+  H.check_switch = (S.use_cheby || S.use_ppcg) ? 1 : 0;
+  H.n = 1;
+  H.status = RUN;
+  H.theta = c->theta;
+  if ((rc = push_state(c))) return rc;
+  {
+    Reduce rd = c->rd();
+    launch_residual(c->f, c->L, &rd, RED_INIT_RESIDUAL, c->stream);
+  }
+  if (S.use_cg || S.use_cheby || S.use_ppcg) {
+    launch_cg_init(c->f, c->L, c->g, c->rd(), RED_RRO, c->stream);
+    if ((rc = do_halo(c, M(TL_FIELD_U) | M(TL_FIELD_P), 1))) return rc;
+  } else if (S.use_jacobi) {
+    launch_jacobi_denominator(c->f, c->L, c->g, c->stream);
+  }
+  if ((rc = check_launch("tea_leaf init"))) return rc;
+  if ((rc = sync_state(c))) return rc;
+  const double initial_residual = H.initial_residual;
+
+  // ---- iteration (tea_solve.f90:152-414) ----
+  int n = 1;
+  double error = 0.0, old_error = H.old_error, rro = H.rro;
+  int cheby_calc_steps = 0, est_itc = 0, ppcg_inner_iters = 0, cg_calc_steps = 0, max_cheby_iters = 0;
+  bool ch_switch_check = false, ppcg_active = false, exited = false;
+  int fields_mask = S.use_jacobi ? M(TL_FIELD_U) : M(TL_FIELD_P);
+  const int batch = tl_ctx::BATCH;
+
+  while (n <= max_iters) {
+    if (!ch_switch_check) {
+      if (cheby_calc_steps > 0)
+        ch_switch_check = true;
+      else if (!c->first && S.use_ppcg && n > 1)
+        ch_switch_check = true;
+      else if (std::fabs(old_error) <= o->ch_cg_epslim && n >= o->ch_cg_presteps)
+        ch_switch_check = true;
+    }
+    const bool cg_phase = (S.use_cg || S.use_cheby || S.use_ppcg) && !((S.use_cheby || S.use_ppcg) && ch_switch_check);
+
+    if (cg_phase) {
+      // device-resident CG loop, batches of iterations, one status read per batch
+      LoopArgs la = c->loop();
+      const int n_before = n;
+      for (int i = 0; i < batch; ++i) {
+        if (c->prof) CK(cudaEventRecord(c->pev[3 * i], c->stream));
+        launch_fused_cg_w(la, false, c->stream);
+        if (c->prof) CK(cudaEventRecord(c->pev[3 * i + 1], c->stream));
+        launch_fused_cg_ur(la, false, c->stream);
+        if (c->prof) CK(cudaEventRecord(c->pev[3 * i + 2], c->stream));
+      }
+      if ((rc = check_launch("cg batch"))) return rc;
+      if ((rc = sync_state(c))) return rc;
+      if (c->prof) {
+        // iterations of this batch that did work (the rest returned on the status word)
+        int ran = (H.status == EXIT_CONVERGED || H.status == EXIT_BREAKDOWN) ? H.n_exit - n_before + 1
+                                                                               : H.n - n_before;
+        ran = std::min(std::max(ran, 0), batch);
+        for (int i = 0; i < ran; ++i) {
+          float a = 0.f, b = 0.f;
+          CK(cudaEventElapsedTime(&a, c->pev[3 * i], c->pev[3 * i + 1]));
+          CK(cudaEventElapsedTime(&b, c->pev[3 * i + 1], c->pev[3 * i + 2]));
+          c->prof_ms[TL_KERNEL_CG_MATVEC] += a;
+          c->prof_ms[TL_KERNEL_CG_UPDATE] += b;
+        }
+        c->prof_n[TL_KERNEL_CG_MATVEC] += ran;
+        c->prof_n[TL_KERNEL_CG_UPDATE] += ran;
+      }
+      cg_calc_steps = H.cg_calc_steps;
+      if (H.status == EXIT_BREAKDOWN) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite CG scalar");
+      error = H.error;
+      old_error = H.old_error;
+      rro = H.rro;
+      if (H.status == EXIT_CONVERGED) {
+        n = H.n_exit;
+        exited = true;
+        break;
+      }
+      n = H.n;
+      if (H.status == EXIT_MAX_ITERS) break;
+      if (H.status == STOP_SWITCH) {
+        H.status = RUN;
+        if ((rc = push_state(c))) return rc;
+      }
+      continue;
+    }
+
+    // ---- Chebyshev / PPCG / Jacobi iteration n (host-driven over the per-kernel path) ----
+    if ((S.use_cheby || S.use_ppcg) && ch_switch_check) {
+      if (cheby_calc_steps == 0) {
+        max_cheby_iters = max_iters - n + 2;
+        if (c->first) {
+          std::vector<double> ha(n - 1 > 0 ? n - 1 : 1), hb(ha.size());
+          if (n - 1 > 0) {
+            CK(cudaMemcpy(ha.data(), c->hist_a + 1, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(hb.data(), c->hist_b + 1, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost));
+          }
+          const int bad = calc_eigenvalues(ha, hb, n - 1, &c->eigmin, &c->eigmax);
+          c->first = 0;
+          if (bad) return fail(TL_ERR_EIGEN, "tea_leaf: Error in calculating eigenvalues");
+          c->eigmin = c->eigmin * 0.95;
+          c->eigmax = c->eigmax * 1.05;
+        }
+        if (S.use_cheby) {
+          calc_ch_coefs(S.ch_a, S.ch_b, c->eigmin, c->eigmax, &c->theta, max_cheby_iters);
+          fields_mask = M(TL_FIELD_U);
+        } else {
+          calc_ch_coefs(S.ch_a, S.ch_b, c->eigmin, c->eigmax, &c->theta, std::max(inner, 0));
+          ppcg_active = true;
+        }
+        if ((int)S.ch_a.size() < inner + 2) {
+          S.ch_a.resize(inner + 2, 0.0);
+          S.ch_b.resize(inner + 2, 0.0);
+        }
+        c->cn = c->eigmax / c->eigmin;
+        // p currently lives in whichever CG buffer the last iteration wrote; step 3 rebuilds p
+        launch_ppcg_init(c->f, c->L, c->g, 2, ppcg_active, c->rd(), RED_STORE, c->stream);
+        if ((rc = S.run_ppcg_inner_steps(inner))) return rc;
+        ppcg_inner_iters += inner;
+        launch_ppcg_init(c->f, c->L, c->g, 3, ppcg_active, c->rd(), RED_STORE, c->stream);
+        if ((rc = check_launch("ppcg_init"))) return rc;
+        if ((rc = reduce_result(c, &rro))) return rc;
+        fields_mask = M(TL_FIELD_P);
+        if ((rc = do_halo(c, fields_mask, 1))) return rc;
+      }
+      if (S.use_cheby) {
+        if (cheby_calc_steps == 0) {
+          double bb;
+          if ((rc = S.norm(c->f.u0, &bb))) return rc;
+          launch_cheby_init(c->f, c->L, c->g, c->theta, c->stream);
+          if ((rc = do_halo(c, fields_mask, 1))) return rc;
+          launch_cheby_iterate(c->f, c->L, c->g, S.ch_a[1], S.ch_b[1], c->stream);
+          if ((rc = S.norm(c->f.r, &old_error))) return rc;
+          const double it_alpha = o->eps / 2.0 * std::sqrt(bb / old_error);
+          const double gamm = (std::sqrt(c->cn) - 1.0) / (std::sqrt(c->cn) + 1.0);
+          est_itc = (int)std::lround(std::log(it_alpha) / std::log(gamm));
+          cheby_calc_steps = 1;
+        } else {
+          launch_cheby_iterate(c->f, c->L, c->g, S.ch_a[cheby_calc_steps], S.ch_b[cheby_calc_steps], c->stream);
+          if (n >= est_itc && n % 10 == 0) {
+            if ((rc = S.norm(c->f.r, &error))) return rc;
+          }
+        }
+      } else {
+        double pw, rrn;
+        launch_cg_calc_w(c->f, c->L, c->rd(), c->stream);
+        if ((rc = reduce_result(c, &pw))) return rc;
+        launch_copy_interior(c->f.r_store, c->f.r, c->L, c->stream);
+        launch_dot(c->f.z, c->f.r, nullptr, c->L, c->rd(), RED_STORE, c->stream);
+        if ((rc = reduce_result(c, &rro))) return rc;
+        const double alpha = rro / pw;
+        launch_cg_calc_ur(c->f, c->L, c->g, alpha, c->rd(), c->stream);
+        if ((rc = S.run_ppcg_inner_steps(inner))) return rc;
+        ppcg_inner_iters += inner;
+        launch_dot(c->f.z, c->f.r, c->f.r_store, c->L, c->rd(), RED_STORE, c->stream);
+        if ((rc = reduce_result(c, &rrn))) return rc;
+        const double beta = rrn / rro;
+        launch_cg_calc_p(c->f, c->L, beta, true, c->stream);
+        error = rrn;
+        rro = rrn;
+      }
+      cheby_calc_steps += 1;
+    } else if (S.use_jacobi) {
+      launch_jacobi(c->f, c->L, c->rd(), c->stream);
+      if ((rc = check_launch("jacobi"))) return rc;
+      if ((rc = reduce_result(c, &error))) return rc;
+    }
+    if ((rc = do_halo(c, fields_mask, 1))) return rc;
+    error = std::sqrt(std::fabs(error));
+    if (std::fabs(error) < o->eps * initial_residual) {
+      exited = true;
+      break;
+    }
+    old_error = error;
+    ++n;
+  }
+  (void)exited;
+
+  double exact_error = 0.0;
+  if (o->check_result) {
+    if ((rc = do_halo(c, M(TL_FIELD_U), 1))) return rc;
+    Reduce rd = c->rd();
+    launch_residual(c->f, c->L, &rd, RED_STORE, c->stream);
+    if ((rc = reduce_result(c, &exact_error))) return rc;
+    exact_error = std::sqrt(exact_error);
+  }
+  launch_finalise(c->f, c->L, c->stream);
+  if ((rc = do_halo(c, M(TL_FIELD_ENERGY1), 1))) return rc;
+  if ((rc = check_launch("finalise"))) return rc;
+  CK(cudaEventRecord(c->ev1, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+
+  info->n_exit = n;
+  info->reported_iterations = n - 1;
+  info->ppcg_inner_iters = ppcg_inner_iters;
+  info->cg_calc_steps = cg_calc_steps;
+  info->cheby_calc_steps = cheby_calc_steps;
+  info->est_itc = est_itc;
+  info->initial_residual = initial_residual;
+  info->error = error;
+  info->exact_error = exact_error;
+  info->eigmin = c->eigmin;
+  info->eigmax = c->eigmax;
+  info->solve_seconds = ms * 1e-3;
+  info->kernel_launches = launch_counter() - launches0;
+  return TL_OK;
+}

@@ -1,0 +1,145 @@
+// tl_device.cuh -- device-side layout, solver state and reduction helpers shared by the
+// TeaLeaf GB300 kernels.
+//
+// Field layout in HBM: every field is a (y_cells + 2) x ld array of FP64, x fastest.
+// Row 0 and row y_cells+1 are the bottom/top halo rows; in each row the interior cell
+// j = 1 sits at column XOFF, so interior rows start on a 128-byte boundary and ld is a
+// multiple of 16 doubles.  Column XOFF-1 is the left halo cell, column XOFF+x_cells the
+// right one.  The one-cell halo holds the reference's reflective-boundary copies
+// (update_halo_kernel.f90:136-195); without reflective_boundary it stays zero and the
+// boundary face coefficients are zero, so halo values never reach the operator.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tl {
+
+constexpr int XOFF = 16;  // column of interior cell j = 1
+
+struct Layout {
+  int nx, ny;  // interior cells
+  int ld;      // row stride (doubles)
+  __host__ __device__ __forceinline__ long long at(int j, int k) const {
+    return (long long)k * ld + (XOFF - 1) + j;
+  }
+  __host__ __device__ __forceinline__ long long elems() const { return (long long)(ny + 2) * ld; }
+};
+
+// Solver fields.  cx = rx*Kx and cy = ry*Ky are the face coefficients pre-scaled once per
+// solve; kx/ky keep the reference's unscaled values.  p2 is the ping-pong partner of p in
+// the fused CG loop; u1 is the partner of u for kernels that read u's neighbours while
+// producing a new u (Chebyshev, Jacobi); sd1 is the partner of sd for the PPCG inner
+// sweeps; jinv = 1/(Jacobi denominator).
+struct Fields {
+  double *density, *energy1, *u, *u0, *r, *w, *p, *p2, *kx, *ky, *cx, *cy, *di, *z, *mi, *sd, *utemp, *rtemp,
+      *r_store, *cp, *bfp, *u1, *sd1, *jinv;
+};
+
+// Exit / stop codes written by the device epilogues.
+enum : int {
+  RUN = 0,
+  EXIT_CONVERGED = 1,
+  EXIT_BREAKDOWN = 2,
+  EXIT_MAX_ITERS = 3,
+  STOP_SWITCH = 4,  // CG presteps done: host computes eigenvalues / coefficients
+};
+
+// Device-resident state of one tea_leaf() solve (tea_solve.f90:42-68).  Written only by
+// the single last-arriving CTA of a reducing kernel (or by the host between launches).
+struct LoopState {
+  double red[4];  // raw results of the last reduction (per-kernel entry points)
+  double rro, pw, rrn, alpha, beta;
+  double error, old_error, initial_residual, eps;
+  double epslim;
+  double theta;
+  int n;           // tea_leaf loop index of the iteration about to run / running
+  int max_iters;
+  int status;      // RUN or an EXIT_* / STOP_* code
+  int n_exit;
+  int p_pending;   // 1: the next CG matvec first applies p = src + beta*p
+  int presteps;
+  int first;       // reference 'first' flag (eigenvalues not yet estimated)
+  int use_ppcg;    // switch rule for PPCG (tea_solve.f90:164)
+  int cheby_step;  // cheby_calc_steps
+  int est_itc;
+  int cg_calc_steps;
+  int check_switch;  // evaluate the CG->Chebyshev/PPCG switch in the CG epilogue
+  int pad[2];
+};
+
+// Launch-independent pointers handed to every kernel that reduces.
+struct Reduce {
+  double* partials;    // [gridDim.x * gridDim.y][NV]
+  unsigned* counter;   // arrival ticket, reset to 0 by the last CTA
+  LoopState* st;
+  double* hist_a;      // cg_alphas(1:max_iters), 1-based
+  double* hist_b;      // cg_betas
+  const double* ch_a;  // Chebyshev / PPCG coefficients, 1-based
+  const double* ch_b;
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block sum of NV values in fixed order; result valid in thread 0.  scratch: 32*NV doubles.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* scratch) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) v[i] = warp_sum(v[i]);
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) scratch[wid * NV + i] = v[i];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      double x = lane < nw ? scratch[lane * NV + i] : 0.0;
+      v[i] = warp_sum(x);
+    }
+  }
+}
+
+// Two-level deterministic grid reduction: every CTA publishes its block sum; the CTA
+// that arrives last sums all partials in block order (thread t takes t, t+T, ...; then a
+// fixed tree), runs epi(total) in thread 0 and re-arms the ticket.  The result does not
+// depend on which CTA arrives last.
+template <int NV, typename Epi>
+__device__ __forceinline__ void grid_reduce(double (&v)[NV], const Reduce& rd, Epi epi) {
+  __shared__ double scratch[32 * NV];
+  __shared__ int is_last;
+  block_sum<NV>(v, scratch);
+  const unsigned nblk = gridDim.x * gridDim.y;
+  const unsigned bid = blockIdx.y * gridDim.x + blockIdx.x;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) rd.partials[(size_t)bid * NV + i] = v[i];
+    __threadfence();
+    const unsigned ticket = atomicAdd(rd.counter, 1u);
+    is_last = (ticket == nblk - 1);
+  }
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  double acc[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) acc[i] = 0.0;
+  for (unsigned b = threadIdx.x; b < nblk; b += blockDim.x) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) acc[i] += __ldcg(rd.partials + (size_t)b * NV + i);
+  }
+  block_sum<NV>(acc, scratch);
+  if (threadIdx.x == 0) {
+    epi(acc);
+    *rd.counter = 0u;
+    __threadfence();
+  }
+}
+
+}  // namespace tl

@@ -1,0 +1,331 @@
+// tl_fused.cu -- fused solver-loop kernels: the iteration bodies of tea_leaf()
+// (tea_solve.f90:152-414) with every solver scalar kept in device memory (LoopState).
+//
+// FP64 CG, per iteration n (tea_solve.f90:341-369):
+//   k_fused_cg_w : p_n = src + beta*p_{n-1} (cg_kernel.f90:306-347, deferred from iteration
+//                  n-1), w = A p_n, pw = p_n.w (cg_kernel.f90:114-156); epilogue alpha = rro/pw.
+//   k_fused_cg_ur: u += alpha p_n, r -= alpha w, rrn = r.r (cg_kernel.f90:198-304); epilogue
+//                  beta = rrn/rro, error = sqrt|rrn|, the EXIT test, n = n+1.
+// p_{n-1} and p_n live in two buffers (P[(n-1)&1] -> P[n&1]) so that the CTA computing a
+// halo row of p_n never sees a neighbour's already-updated value.
+//
+// The matvec kernel marches up a strip of 2*FT columns, one row per step: each thread owns
+// two adjacent columns (16-byte loads), keeps p of rows k-1, k, k+1 in registers and swaps
+// row k through shared memory for the horizontal neighbours; the two strip-edge columns
+// and the first/last row of a CTA are recomputed (p = src + beta*p costs one FMA).  Off the
+// domain the neighbour is the mirror value (the reference's reflective halo copy of p, or a
+// value multiplied by a zero boundary coefficient otherwise).
+#include "tl_kernels.cuh"
+
+namespace tl {
+
+namespace {
+
+constexpr int FT = 128;      // threads per CTA
+constexpr int SW = 2 * FT;   // strip width (columns)
+
+__device__ __forceinline__ void finish_iteration(LoopState* st, double err_raw) {
+  const double err = sqrt(fabs(err_raw));
+  st->error = err;
+  if (!isfinite(err)) {
+    st->status = EXIT_BREAKDOWN;
+    st->n_exit = st->n;
+    return;
+  }
+  if (fabs(err) < st->eps * st->initial_residual) {
+    st->status = EXIT_CONVERGED;
+    st->n_exit = st->n;
+    return;
+  }
+  st->old_error = err;
+  st->n += 1;
+  if (st->n > st->max_iters) {
+    st->status = EXIT_MAX_ITERS;
+    st->n_exit = st->n;
+    return;
+  }
+  if (st->check_switch) {
+    // tea_solve.f90:160-174 evaluated for the next iteration (cheby_calc_steps == 0 here)
+    const bool sw = (!st->first && st->use_ppcg && st->n > 1) ||
+                    (fabs(st->old_error) <= st->epslim && st->n >= st->presteps);
+    if (sw) st->status = STOP_SWITCH;
+  }
+}
+
+struct EpiCgW {
+  Reduce rd;
+  bool ppcg;
+  __device__ void operator()(double (&acc)[2]) const {
+    LoopState* st = rd.st;
+    st->pw = acc[0];
+    if (ppcg) st->rro = acc[1];  // tea_leaf_ppcg_calc_zrnorm, allsum2 (tea_solve.f90:300-303)
+    const double alpha = st->rro / st->pw;
+    st->alpha = alpha;
+    if (!ppcg) rd.hist_a[st->n] = alpha;
+    if (!isfinite(alpha)) {
+      st->status = EXIT_BREAKDOWN;
+      st->n_exit = st->n;
+    }
+  }
+};
+
+struct EpiCgUr {
+  Reduce rd;
+  __device__ void operator()(double (&acc)[1]) const {
+    LoopState* st = rd.st;
+    const double rrn = acc[0];
+    st->rrn = rrn;
+    const double beta = rrn / st->rro;
+    st->beta = beta;
+    rd.hist_b[st->n] = beta;
+    st->p_pending = 1;
+    st->rro = rrn;
+    st->cg_calc_steps += 1;
+    finish_iteration(st, rrn);
+  }
+};
+
+// p_new for two adjacent columns (ja, ja+1) of row k
+struct PNew {
+  const double* __restrict__ src;
+  const double* __restrict__ pold;
+  double beta;
+  bool upd;
+  __device__ __forceinline__ double2 pair(long long c) const {
+    double2 q = __ldg(reinterpret_cast<const double2*>(pold + c));
+    if (upd) {
+      const double2 s = __ldg(reinterpret_cast<const double2*>(src + c));
+      q.x = fma(beta, q.x, s.x);
+      q.y = fma(beta, q.y, s.y);
+    }
+    return q;
+  }
+  __device__ __forceinline__ double one(long long c) const {
+    const double q = __ldg(pold + c);
+    return upd ? fma(beta, q, __ldg(src + c)) : q;
+  }
+};
+
+template <bool PPCG>
+__global__ void __launch_bounds__(FT) k_fused_cg_w(LoopArgs a, int rows_per_cta) {
+  LoopState* st = a.rd.st;
+  if (st->status != RUN) return;
+  const Layout L = a.L;
+  const int n = st->n;
+  const bool use_z = PPCG || a.precond != 1;
+  PNew pn_{use_z ? a.f.z : a.f.r, (n & 1) ? a.f.p : a.f.p2, st->beta, st->p_pending != 0};
+  double* __restrict__ pout = (n & 1) ? a.f.p2 : a.f.p;
+  double* __restrict__ w = a.f.w;
+  const double* __restrict__ cx = a.f.cx;
+  const double* __restrict__ cy = a.f.cy;
+  const double* __restrict__ di = a.f.di;
+
+  __shared__ double buf[2][SW + 2];
+  const int t = threadIdx.x;
+  const int js = blockIdx.x * SW + 1;
+  const int ja = js + 2 * t;
+  const bool active = ja <= L.nx;
+  const bool has_b = ja + 1 <= L.nx;
+  const int k0 = blockIdx.y * rows_per_cta + 1;
+  const int k1 = min(k0 + rows_per_cta - 1, L.ny);
+  const int ld = L.ld;
+
+  double acc[2] = {0.0, 0.0};
+  double2 pm = make_double2(0.0, 0.0), pc = pm, pnx = pm, cyc = pm;
+  if (active) {
+    pc = pn_.pair(L.at(ja, k0));
+    pm = (k0 == 1) ? pc : pn_.pair(L.at(ja, k0 - 1));
+    cyc = *reinterpret_cast<const double2*>(cy + L.at(ja, k0));
+  }
+  for (int k = k0; k <= k1; ++k) {
+    const int b = k & 1;
+    if (active) {
+      pnx = (k == L.ny) ? pc : pn_.pair(L.at(ja, k + 1));
+      buf[b][2 * t + 1] = pc.x;
+      buf[b][2 * t + 2] = pc.y;
+    }
+    if (t == 0 && js > 1) buf[b][0] = pn_.one(L.at(js - 1, k));
+    if (t == FT - 1 && js + SW <= L.nx) buf[b][SW + 1] = pn_.one(L.at(js + SW, k));
+    __syncthreads();
+    if (active) {
+      const long long c = L.at(ja, k);
+      const double2 cyn = *reinterpret_cast<const double2*>(cy + c + ld);
+      const double2 cxa = *reinterpret_cast<const double2*>(cx + c);
+      const double2 dd = *reinterpret_cast<const double2*>(di + c);
+      const double left_a = (ja == 1) ? pc.x : buf[b][ja - js];
+      const double right_a = has_b ? pc.y : pc.x;
+      double wa = dd.x * pc.x;
+      wa = fma(-cyn.x, pnx.x, wa);
+      wa = fma(-cyc.x, pm.x, wa);
+      wa = fma(-cxa.y, right_a, wa);
+      wa = fma(-cxa.x, left_a, wa);
+      acc[0] = fma(wa, pc.x, acc[0]);
+      if (has_b) {
+        const double cxr = cx[c + 2];
+        const double right_b = (ja + 1 == L.nx) ? pc.y : buf[b][ja - js + 3];
+        double wb = dd.y * pc.y;
+        wb = fma(-cyn.y, pnx.y, wb);
+        wb = fma(-cyc.y, pm.y, wb);
+        wb = fma(-cxr, right_b, wb);
+        wb = fma(-cxa.y, pc.x, wb);
+        acc[0] = fma(wb, pc.y, acc[0]);
+        *reinterpret_cast<double2*>(w + c) = make_double2(wa, wb);
+        *reinterpret_cast<double2*>(pout + c) = pc;
+      } else {
+        w[c] = wa;
+        pout[c] = pc.x;
+      }
+      if (PPCG) {
+        // tea_leaf_ppcg_store_r (ppcg_kernel.f90:507-530) and calc_zrnorm z.r (:411-451)
+        const double2 rr = *reinterpret_cast<const double2*>(a.f.r + c);
+        const double2 zz = *reinterpret_cast<const double2*>(a.f.z + c);
+        a.f.r_store[c] = rr.x;
+        acc[1] = fma(zz.x, rr.x, acc[1]);
+        if (has_b) {
+          a.f.r_store[c + 1] = rr.y;
+          acc[1] = fma(zz.y, rr.y, acc[1]);
+        }
+      }
+      cyc = cyn;
+    }
+    pm = pc;
+    pc = pnx;
+  }
+  grid_reduce<2>(acc, a.rd, EpiCgW{a.rd, PPCG});
+}
+
+// u += alpha p_n, r -= alpha w, then by MODE:
+//   UR_CG    r.r (or r.z with z = Mi r for jac_diag) and the CG epilogue;
+//   UR_PPCG  no reduction (rrn is discarded, tea_solve.f90:309-311), fused init_sd;
+//   UR_ONLY  no reduction: the block-Jacobi solve and r.z follow in k_fused_block_rz.
+enum { UR_CG = 0, UR_PPCG = 1, UR_ONLY = 2 };
+template <int MODE>
+__global__ void __launch_bounds__(FT) k_fused_cg_ur(LoopArgs a) {
+  constexpr bool PPCG = MODE == UR_PPCG;
+  LoopState* st = a.rd.st;
+  if (st->status != RUN) return;
+  const Layout L = a.L;
+  const int n = st->n;
+  const double alpha = st->alpha;
+  const double* __restrict__ p = (n & 1) ? a.f.p2 : a.f.p;
+  const int ja = blockIdx.x * SW + 1 + 2 * threadIdx.x;
+  const bool has_b = ja + 1 <= L.nx;
+  const double theta_r = PPCG ? 1.0 / st->theta : 0.0;
+  double acc[1] = {0.0};
+  if (ja <= L.nx) {
+    for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
+      const long long c = L.at(ja, k);
+      const double2 pp = *reinterpret_cast<const double2*>(p + c);
+      const double2 ww = *reinterpret_cast<const double2*>(a.f.w + c);
+      double2 uu = *reinterpret_cast<const double2*>(a.f.u + c);
+      double2 rr = *reinterpret_cast<const double2*>(a.f.r + c);
+      uu.x = fma(alpha, pp.x, uu.x);
+      uu.y = fma(alpha, pp.y, uu.y);
+      rr.x = fma(-alpha, ww.x, rr.x);
+      rr.y = fma(-alpha, ww.y, rr.y);
+      double2 zz = rr;
+      if (a.precond == 2) {
+        const double2 mi = *reinterpret_cast<const double2*>(a.f.mi + c);
+        zz.x = mi.x * rr.x;
+        zz.y = mi.y * rr.y;
+      }
+      if (has_b) {
+        *reinterpret_cast<double2*>(a.f.u + c) = uu;
+        *reinterpret_cast<double2*>(a.f.r + c) = rr;
+        if (a.precond == 2) *reinterpret_cast<double2*>(a.f.z + c) = zz;
+      } else {
+        a.f.u[c] = uu.x;
+        a.f.r[c] = rr.x;
+        if (a.precond == 2) a.f.z[c] = zz.x;
+      }
+      if (MODE == UR_CG) {
+        acc[0] = fma(rr.x, zz.x, acc[0]);
+        if (has_b) acc[0] = fma(rr.y, zz.y, acc[0]);
+      } else if (MODE == UR_PPCG) {
+        // tea_leaf_kernel_ppcg_init_sd (ppcg_kernel.f90:31-88): sd = (z|r)/theta, rtemp = r, utemp = sd
+        const double2 s = make_double2(zz.x * theta_r, zz.y * theta_r);
+        if (has_b) {
+          *reinterpret_cast<double2*>(a.f.sd + c) = s;
+          *reinterpret_cast<double2*>(a.f.rtemp + c) = rr;
+          *reinterpret_cast<double2*>(a.f.utemp + c) = s;
+        } else {
+          a.f.sd[c] = s.x;
+          a.f.rtemp[c] = rr.x;
+          a.f.utemp[c] = s.x;
+        }
+      }
+    }
+  }
+  if (MODE == UR_CG) grid_reduce<1>(acc, a.rd, EpiCgUr{a.rd});
+}
+
+// Block-Jacobi CG tail (cg_kernel.f90:256-283): z = M^-1 r with the 4-row tridiagonal
+// blocks of tea_block_solve (common_kernel.f90:378-468), r.z, and the CG epilogue.
+// One thread per column and 4-row block; blocks of rows strided over gridDim.y.
+__global__ void __launch_bounds__(FT) k_fused_block_rz(LoopArgs a, double ry) {
+  LoopState* st = a.rd.st;
+  if (st->status != RUN) return;
+  const Layout L = a.L;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  double acc[1] = {0.0};
+  if (j <= L.nx) {
+    for (int bottom = blockIdx.y * 4 + 1; bottom <= L.ny; bottom += gridDim.y * 4) {
+      const int top = min(bottom + 3, L.ny);
+      double dp[4], zl[4], rv[4];
+      long long c = L.at(j, bottom);
+      rv[0] = a.f.r[c];
+      dp[0] = rv[0] / a.f.di[c];
+      for (int k = bottom + 1; k <= top; ++k) {
+        c = L.at(j, k);
+        rv[k - bottom] = a.f.r[c];
+        dp[k - bottom] = (rv[k - bottom] - (-a.f.ky[c] * ry) * dp[k - bottom - 1]) * a.f.bfp[c];
+      }
+      zl[top - bottom] = dp[top - bottom];
+      for (int k = top - 1; k >= bottom; --k) zl[k - bottom] = dp[k - bottom] - a.f.cp[L.at(j, k)] * zl[k - bottom + 1];
+      for (int k = bottom; k <= top; ++k) {
+        a.f.z[L.at(j, k)] = zl[k - bottom];
+        acc[0] = fma(rv[k - bottom], zl[k - bottom], acc[0]);
+      }
+    }
+  }
+  grid_reduce<1>(acc, a.rd, EpiCgUr{a.rd});
+}
+
+inline int strips(const Layout& L) { return (L.nx + SW - 1) / SW; }
+
+}  // namespace
+
+void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s) {
+  const int ns = strips(a.L);
+  // aim for >= ~8 CTAs per SM of 152, with 8..64 rows per CTA
+  int rows = (int)(((long long)a.L.ny * ns) / (152 * 8));
+  rows = rows < 8 ? 8 : (rows > 64 ? 64 : rows);
+  const int min_rows = (int)(((long long)a.L.ny * ns + MAX_REDUCE_BLOCKS - 1) / MAX_REDUCE_BLOCKS);
+  if (rows < min_rows) rows = min_rows;  // keep the CTA count within the partials buffer
+  dim3 grid(ns, (a.L.ny + rows - 1) / rows);
+  if (ppcg)
+    { ++launch_counter(); k_fused_cg_w<true><<<grid, FT, 0, s>>>(a, rows); }
+  else
+    { ++launch_counter(); k_fused_cg_w<false><<<grid, FT, 0, s>>>(a, rows); }
+}
+
+void launch_fused_cg_ur(const LoopArgs& a, bool ppcg, cudaStream_t s) {
+  const int ns = strips(a.L);
+  int gy = a.L.ny < 512 ? a.L.ny : 512;
+  if ((long long)gy * ns > MAX_REDUCE_BLOCKS) gy = MAX_REDUCE_BLOCKS / ns;
+  dim3 grid(ns, gy);
+  if (ppcg) {
+    { ++launch_counter(); k_fused_cg_ur<UR_PPCG><<<grid, FT, 0, s>>>(a); }
+  } else if (a.precond == 3) {
+    { ++launch_counter(); k_fused_cg_ur<UR_ONLY><<<grid, FT, 0, s>>>(a); }
+    const int gx = (a.L.nx + FT - 1) / FT;
+    int by = (a.L.ny + 3) / 4;
+    if (by > 1024) by = 1024;
+    if ((long long)by * gx > MAX_REDUCE_BLOCKS) by = MAX_REDUCE_BLOCKS / gx;
+    { ++launch_counter(); k_fused_block_rz<<<dim3(gx, by), FT, 0, s>>>(a, a.ry); }
+  } else {
+    { ++launch_counter(); k_fused_cg_ur<UR_CG><<<grid, FT, 0, s>>>(a); }
+  }
+}
+
+}  // namespace tl

@@ -1,0 +1,77 @@
+// tl_kernels.cuh -- host-side launchers of the TeaLeaf GB300 kernels (defined in
+// tl_kernels.cu, tl_fused.cu).  All launchers are asynchronous on the given stream.
+#pragma once
+
+#include "tl_device.cuh"
+
+namespace tl {
+
+struct Geometry {
+  double rx, ry;   // dt/dx^2, dt/dy^2
+  double dx, dy;   // cell widths
+  int coefficient, precond, reflective;
+};
+
+// Capacity of the per-CTA partials buffer (CTAs x 4 lanes).
+constexpr int MAX_REDUCE_BLOCKS = 65536;
+
+// Number of kernels the launchers below have launched on the calling thread.
+long long& launch_counter();
+
+// ---- set-up, summary, generation, halo ----------------------------------
+void launch_init_faces(const Fields& f, const Layout& L, const Geometry& g, cudaStream_t s);
+void launch_init_cells(const Fields& f, const Layout& L, const Geometry& g, bool with_residual, cudaStream_t s);
+void launch_block_init(const Fields& f, const Layout& L, const Geometry& g, cudaStream_t s);
+void launch_generate(const Fields& f, const Layout& L, int nstates, const double* states /*device, 8*nstates*/,
+                     double xmin, double ymin, double dx, double dy, cudaStream_t s);
+void launch_field_summary(const Fields& f, const Layout& L, double cell_vol, const Reduce& rd, cudaStream_t s);
+void launch_update_halo(double* const* fields, int nfields, const Layout& L, cudaStream_t s);
+void launch_copy_interior(double* dst, const double* src, const Layout& L, cudaStream_t s);
+void launch_copy_all(double* dst, const double* src, const Layout& L, cudaStream_t s);
+
+// ---- per-kernel entry points (reference semantics) ----------------------
+// Reduction epilogue modes
+enum RedMode : int {
+  RED_STORE = 0,          // st->red[0..NV) = totals
+  RED_INIT_RESIDUAL = 1,  // old_error = rr, initial_residual = sqrt(|rr|)
+  RED_RRO = 2,            // st->rro = total
+  RED_EXACT = 3,          // st->red[0] = total (exact residual)
+};
+void launch_residual(const Fields& f, const Layout& L, const Reduce* rd /*null: no norm*/, int mode, cudaStream_t s);
+void launch_norm2(const double* a, const Layout& L, const Reduce& rd, int mode, cudaStream_t s);
+void launch_finalise(const Fields& f, const Layout& L, cudaStream_t s);
+void launch_precond(const Fields& f, const Layout& L, const Geometry& g, const double* src, double* dst,
+                    cudaStream_t s);
+void launch_cg_init(const Fields& f, const Layout& L, const Geometry& g, const Reduce& rd, int mode, cudaStream_t s);
+void launch_cg_calc_w(const Fields& f, const Layout& L, const Reduce& rd, cudaStream_t s);
+void launch_cg_calc_ur(const Fields& f, const Layout& L, const Geometry& g, double alpha, const Reduce& rd,
+                       cudaStream_t s);
+void launch_cg_calc_p(const Fields& f, const Layout& L, double beta, bool use_z, cudaStream_t s);
+void launch_cheby_init(const Fields& f, const Layout& L, const Geometry& g, double theta, cudaStream_t s);
+void launch_cheby_iterate(const Fields& f, const Layout& L, const Geometry& g, double a, double b, cudaStream_t s);
+void launch_ppcg_init_sd(const Fields& f, const Layout& L, const Geometry& g, double theta, cudaStream_t s);
+void launch_ppcg_init(const Fields& f, const Layout& L, const Geometry& g, int step, bool ppcg_active,
+                      const Reduce& rd, int mode, cudaStream_t s);
+void launch_ppcg_inner(const Fields& f, const Layout& L, const Geometry& g, double a, double b, cudaStream_t s);
+void launch_dot(const double* a, const double* b, const double* bminus /*nullable*/, const Layout& L,
+                const Reduce& rd, int mode, cudaStream_t s);
+void launch_jacobi(const Fields& f, const Layout& L, const Reduce& rd, cudaStream_t s);
+
+// ---- fused solver loop (device-resident scalars) ------------------------
+struct LoopArgs {
+  Fields f;
+  Layout L;
+  Reduce rd;
+  int precond;
+  int reflective;
+  double ry;  // dt/dy^2 (block-Jacobi tridiagonal coefficients)
+};
+void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s);
+void launch_fused_cg_ur(const LoopArgs& a, bool ppcg, cudaStream_t s);
+void launch_fused_cheby(const LoopArgs& a, const double* u_in, double* u_out, cudaStream_t s);
+void launch_fused_ppcg_inner(const LoopArgs& a, const double* sd_in, double* sd_out, int step, bool last,
+                             cudaStream_t s);
+void launch_fused_jacobi(const LoopArgs& a, const double* un, double* u_out, cudaStream_t s);
+void launch_jacobi_denominator(const Fields& f, const Layout& L, const Geometry& g, cudaStream_t s);
+
+}  // namespace tl

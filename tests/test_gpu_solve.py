@@ -1,0 +1,125 @@
+"""Whole-solve parity on the GPU.
+
+* The reference's own benchmark decks (Benchmarks/tea_bm_{1..6}.in, CG, tl_eps 1e-15):
+  the step-10 field summary must match the reference's printed values to 1e-10 relative
+  and every per-step iteration count to within one iteration (reduction order differs).
+* Synthetic decks of every solver, coefficient and preconditioner: field summaries within
+  1e-10 and per-cell u within 1e-8 of the oracle run on the same deck (the accuracy bar of
+  the FP64 form), iteration counts within a few percent.
+"""
+import numpy as np
+import pytest
+
+from helpers import small_deck
+from tealeaf_ref_gb300 import deck as dk
+
+pytestmark = pytest.mark.gpu
+
+
+def _summary_close(a, b, rtol):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.all(np.abs(a - b) <= rtol * np.abs(b)), np.max(np.abs(a - b) / np.abs(b))
+
+
+@pytest.mark.parametrize("bm", [1, 2, 3, 4, 5, 6])
+def test_reference_benchmark_decks(golden, bm):
+    from tealeaf_ref_gb300 import native
+
+    g = golden["benchmarks"]["tea_bm_%d" % bm]
+    d = dk.parse_deck(g["deck"])
+    res = native.run_deck(d)
+    want = g["summaries"][-1]
+    step, s = res.summaries[-1]
+    assert step == want["step"]
+    got = [s[0], s[1], s[2], s[3]]
+    ref = [want["volume"], want["mass"], want["energy"], want["temperature"]]
+    ok, worst = _summary_close(got, ref, 1e-10)
+    assert ok, "field summary rel diff %.3e" % worst
+    its = [x["reported_iterations"] for x in res.solves]
+    assert len(its) == len(g["iterations"])
+    for a, b in zip(its, g["iterations"]):
+        assert abs(a - b) <= max(1, int(0.002 * b)), (its, g["iterations"])
+
+
+SOLVE_CASES = [
+    dict(solver="cg"),
+    dict(solver="cg", coefficient=1),
+    dict(solver="cg", precond="jac_diag"),
+    dict(solver="cg", precond="jac_block"),
+    dict(solver="cg", reflective=True),
+    dict(solver="chebyshev", ch_cg_presteps=20),
+    dict(solver="chebyshev", ch_cg_presteps=20, precond="jac_diag"),
+    dict(solver="ppcg", ppcg_inner_steps=10, ch_cg_presteps=20),
+    dict(solver="ppcg", ppcg_inner_steps=10, ch_cg_presteps=20, halo_depth=2),
+    dict(solver="ppcg", ppcg_inner_steps=6, ch_cg_presteps=15, precond="jac_block"),
+    dict(solver="ppcg", ppcg_inner_steps=8, ch_cg_presteps=20, reflective=True),
+    dict(solver="jacobi", max_iters=300, eps=1e-10),
+]
+
+
+@pytest.mark.parametrize("case", SOLVE_CASES, ids=["-".join("%s%s" % kv for kv in c.items()) for c in SOLVE_CASES])
+def test_solvers_against_oracle(case):
+    from oracle import oracle
+    from tealeaf_ref_gb300 import native
+
+    kw = dict(nx=67, ny=45, steps=3, n_rect=4, n_circ=2)
+    kw.update(case)
+    d = small_deck(**kw)
+    ro = oracle.run_deck(d)
+    with native.Chunk.from_deck(d) as c:
+        sums = [c.field_summary()]
+        infos = []
+        for _ in range(d.end_step):
+            infos.append(c.tea_leaf(d))
+        sums.append(c.field_summary())
+        u_gpu = c.download("u")
+    o = oracle.Chunk.from_deck(d)
+    for _ in range(d.end_step):
+        o.tea_leaf(d)
+    u_ref = np.array(o.interior("u"))
+    ok, worst = _summary_close(sums[-1], ro.summaries[-1][1], 1e-10)
+    assert ok, "summary rel diff %.3e" % worst
+    rel = np.max(np.abs(u_gpu - u_ref) / np.abs(u_ref))
+    assert rel < 1e-8, "per-cell u rel diff %.3e" % rel
+    for gi, oi in zip(infos, ro.solves):
+        n_o = oi.reported_iterations
+        # Chebyshev tests its residual only every 10th iteration (tea_solve.f90:273)
+        slack = 10 if d.solver == "chebyshev" else max(2, int(0.03 * n_o))
+        assert abs(gi.reported_iterations - n_o) <= slack, (gi.reported_iterations, n_o)
+
+
+def test_config1_256_against_oracle():
+    """Synthetic config 1 (256^2, 3 rectangles, reciprocal-density keyword, CG, 10 steps)."""
+    from oracle import oracle
+    from tealeaf_ref_gb300 import native
+
+    d = dk.config_deck(1)
+    ro = oracle.run_deck(d)
+    rg = native.run_deck(d)
+    ok, worst = _summary_close(rg.summaries[-1][1], ro.summaries[-1][1], 1e-10)
+    assert ok, worst
+    for gi, oi in zip(rg.solves, ro.solves):
+        assert abs(gi["reported_iterations"] - oi.reported_iterations) <= 2
+
+
+def test_repeatable_bitwise():
+    """Fixed-order reductions: two identical runs give identical bits."""
+    from tealeaf_ref_gb300 import native
+
+    d = small_deck(nx=129, ny=77, steps=2)
+    a = native.run_deck(d).summaries[-1][1]
+    b = native.run_deck(d).summaries[-1][1]
+    np.testing.assert_array_equal(a, b)
+
+
+def test_breakdown_reported():
+    """Zero energy everywhere gives u0 = 0 and r = 0 exactly, so pw = 0 and alpha = 0/0:
+    reported as TL_ERR_BREAKDOWN instead of iterating on NaNs as the reference would."""
+    from tealeaf_ref_gb300 import native
+
+    d = small_deck(nx=16, ny=16, n_rect=0, n_circ=0)
+    d.states[0].energy = 0.0
+    with native.Chunk.from_deck(d) as c:
+        with pytest.raises(native.TeaLeafError) as e:
+            c.tea_leaf(d)
+        assert e.value.code == -4

@@ -121,6 +121,11 @@ int tl_set_device(int device);
 /* Total device bytes the context holds. */
 int tl_device_bytes(const tl_ctx* ctx, unsigned long long* bytes);
 
+/* Page-lock (register) an existing host array so that uploads/downloads run at full link
+ * speed without staging -- e.g. the Fortran driver's density/energy1 arrays.  bytes > 0. */
+int tl_host_register(void* host, unsigned long long bytes);
+int tl_host_unregister(void* host);
+
 /* Host <-> device copies of one field's interior (x_cells x y_cells, leading dimension ld). */
 int tl_upload_field(tl_ctx* ctx, int field, const double* host, int ld);
 int tl_download_field(tl_ctx* ctx, int field, double* host, int ld);

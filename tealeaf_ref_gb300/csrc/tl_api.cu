@@ -370,6 +370,18 @@ int tl_destroy(tl_ctx* c) {
   return TL_OK;
 }
 
+int tl_host_register(void* host, unsigned long long bytes) {
+  if (!host || bytes == 0) return fail(TL_ERR_ARG, "tl_host_register: null pointer or zero size");
+  CK(cudaHostRegister(host, (size_t)bytes, cudaHostRegisterDefault));
+  return TL_OK;
+}
+
+int tl_host_unregister(void* host) {
+  if (!host) return fail(TL_ERR_ARG, "tl_host_unregister: null pointer");
+  CK(cudaHostUnregister(host));
+  return TL_OK;
+}
+
 int tl_device_bytes(const tl_ctx* c, unsigned long long* bytes) {
   if (!c || !bytes) return fail(TL_ERR_ARG, "tl_device_bytes: null argument");
   *bytes = c->slab_bytes + sizeof(double) * 4 * MAX_REDUCE_BLOCKS + 256 + sizeof(LoopState) +
@@ -811,6 +823,11 @@ extern "C" int tl_tea_leaf(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solv
       }
       cg_calc_steps = H.cg_calc_steps;
       if (H.status == EXIT_BREAKDOWN) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite CG scalar");
+      if (H.status != RUN) {
+        // the CG phase stops here: apply the deferred u += alpha p of its last iteration
+        launch_flush_u(la, c->stream);
+        H.u_pending = 0;
+      }
       error = H.error;
       old_error = H.old_error;
       rro = H.rro;

@@ -65,7 +65,12 @@ struct LoopState {
   int est_itc;
   int cg_calc_steps;
   int check_switch;  // evaluate the CG->Chebyshev/PPCG switch in the CG epilogue
-  int pad[2];
+  // Deferred solution update u += u_alpha * P[u_psel] (cg_kernel.f90:286-291 of the previous
+  // iteration): applied by the next matvec sweep, which reads that p anyway, or by the
+  // flush kernel when the CG phase ends.  The same operands, so the same bits.
+  int u_pending;
+  int u_psel;
+  double u_alpha;
 };
 
 // Launch-independent pointers handed to every kernel that reduces.

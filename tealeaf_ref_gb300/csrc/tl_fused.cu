@@ -57,6 +57,7 @@ struct EpiCgW {
   bool ppcg;
   __device__ void operator()(double (&acc)[2]) const {
     LoopState* st = rd.st;
+    st->u_pending = 0;  // every CTA applied the deferred u update for its cells
     st->pw = acc[0];
     if (ppcg) st->rro = acc[1];  // tea_leaf_ppcg_calc_zrnorm, allsum2 (tea_solve.f90:300-303)
     const double alpha = st->rro / st->pw;
@@ -79,6 +80,9 @@ struct EpiCgUr {
     st->beta = beta;
     rd.hist_b[st->n] = beta;
     st->p_pending = 1;
+    st->u_pending = 1;  // u += alpha_n p_n, applied by the next matvec sweep or the flush
+    st->u_alpha = st->alpha;
+    st->u_psel = st->n & 1;
     st->rro = rrn;
     st->cg_calc_steps += 1;
     finish_iteration(st, rrn);
@@ -93,6 +97,17 @@ struct PNew {
   bool upd;
   __device__ __forceinline__ double2 pair(long long c) const {
     double2 q = __ldg(reinterpret_cast<const double2*>(pold + c));
+    if (upd) {
+      const double2 s = __ldg(reinterpret_cast<const double2*>(src + c));
+      q.x = fma(beta, q.x, s.x);
+      q.y = fma(beta, q.y, s.y);
+    }
+    return q;
+  }
+  // same, also returning p_old
+  __device__ __forceinline__ double2 pair(long long c, double2& old) const {
+    old = __ldg(reinterpret_cast<const double2*>(pold + c));
+    double2 q = old;
     if (upd) {
       const double2 s = __ldg(reinterpret_cast<const double2*>(src + c));
       q.x = fma(beta, q.x, s.x);
@@ -130,17 +145,28 @@ __global__ void __launch_bounds__(FT) k_fused_cg_w(LoopArgs a, int rows_per_cta)
   const int k1 = min(k0 + rows_per_cta - 1, L.ny);
   const int ld = L.ld;
 
+  // deferred u += alpha_{n-1} p_{n-1} of the previous iteration (p_{n-1} is pold here)
+  const bool upd_u = !PPCG && st->u_pending != 0;
+  const double ua = st->u_alpha;
+  double* __restrict__ u = a.f.u;
+
   double acc[2] = {0.0, 0.0};
-  double2 pm = make_double2(0.0, 0.0), pc = pm, pnx = pm, cyc = pm;
+  double2 pm = make_double2(0.0, 0.0), pc = pm, pnx = pm, cyc = pm, oc = pm, onx = pm;
   if (active) {
-    pc = pn_.pair(L.at(ja, k0));
+    pc = pn_.pair(L.at(ja, k0), oc);
     pm = (k0 == 1) ? pc : pn_.pair(L.at(ja, k0 - 1));
     cyc = *reinterpret_cast<const double2*>(cy + L.at(ja, k0));
   }
   for (int k = k0; k <= k1; ++k) {
     const int b = k & 1;
     if (active) {
-      pnx = (k == L.ny) ? pc : pn_.pair(L.at(ja, k + 1));
+      if (k == L.ny) {
+        pnx = pc;
+      } else if (k == k1) {
+        pnx = pn_.pair(L.at(ja, k + 1));  // halo row of this CTA: p_new only
+      } else {
+        pnx = pn_.pair(L.at(ja, k + 1), onx);
+      }
       buf[b][2 * t + 1] = pc.x;
       buf[b][2 * t + 2] = pc.y;
     }
@@ -171,9 +197,16 @@ __global__ void __launch_bounds__(FT) k_fused_cg_w(LoopArgs a, int rows_per_cta)
         acc[0] = fma(wb, pc.y, acc[0]);
         *reinterpret_cast<double2*>(w + c) = make_double2(wa, wb);
         *reinterpret_cast<double2*>(pout + c) = pc;
+        if (upd_u) {
+          double2 uu = *reinterpret_cast<const double2*>(u + c);
+          uu.x = fma(ua, oc.x, uu.x);
+          uu.y = fma(ua, oc.y, uu.y);
+          *reinterpret_cast<double2*>(u + c) = uu;
+        }
       } else {
         w[c] = wa;
         pout[c] = pc.x;
+        if (upd_u) u[c] = fma(ua, oc.x, u[c]);
       }
       if (PPCG) {
         // tea_leaf_ppcg_store_r (ppcg_kernel.f90:507-530) and calc_zrnorm z.r (:411-451)
@@ -190,14 +223,33 @@ __global__ void __launch_bounds__(FT) k_fused_cg_w(LoopArgs a, int rows_per_cta)
     }
     pm = pc;
     pc = pnx;
+    oc = onx;
   }
   grid_reduce<2>(acc, a.rd, EpiCgW{a.rd, PPCG});
 }
 
-// u += alpha p_n, r -= alpha w, then by MODE:
-//   UR_CG    r.r (or r.z with z = Mi r for jac_diag) and the CG epilogue;
-//   UR_PPCG  no reduction (rrn is discarded, tea_solve.f90:309-311), fused init_sd;
-//   UR_ONLY  no reduction: the block-Jacobi solve and r.z follow in k_fused_block_rz.
+// Applies a pending deferred u update (LoopState::u_pending) when the CG loop stops.
+__global__ void __launch_bounds__(FT) k_flush_u(LoopArgs a) {
+  const LoopState* st = a.rd.st;
+  if (!st->u_pending) return;
+  const Layout L = a.L;
+  const double* __restrict__ p = st->u_psel ? a.f.p2 : a.f.p;
+  const double ua = st->u_alpha;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (j > L.nx) return;
+  for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
+    const long long c = L.at(j, k);
+    a.f.u[c] = fma(ua, p[c], a.f.u[c]);
+  }
+}
+
+// r -= alpha w (and u += alpha p_n for PPCG), then by MODE:
+//   UR_CG    r.r (or r.z with z = Mi r for jac_diag) and the CG epilogue; u += alpha p_n is
+//            left pending for the next matvec sweep (LoopState::u_pending);
+//   UR_PPCG  u updated here, no reduction (rrn is discarded, tea_solve.f90:309-311), fused
+//            init_sd of the inner sweeps;
+//   UR_ONLY  as UR_CG without the reduction: the block-Jacobi solve and r.z follow in
+//            k_fused_block_rz.
 enum { UR_CG = 0, UR_PPCG = 1, UR_ONLY = 2 };
 template <int MODE>
 __global__ void __launch_bounds__(FT) k_fused_cg_ur(LoopArgs a) {
@@ -215,12 +267,18 @@ __global__ void __launch_bounds__(FT) k_fused_cg_ur(LoopArgs a) {
   if (ja <= L.nx) {
     for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
       const long long c = L.at(ja, k);
-      const double2 pp = *reinterpret_cast<const double2*>(p + c);
       const double2 ww = *reinterpret_cast<const double2*>(a.f.w + c);
-      double2 uu = *reinterpret_cast<const double2*>(a.f.u + c);
       double2 rr = *reinterpret_cast<const double2*>(a.f.r + c);
-      uu.x = fma(alpha, pp.x, uu.x);
-      uu.y = fma(alpha, pp.y, uu.y);
+      if (PPCG) {
+        const double2 pp = *reinterpret_cast<const double2*>(p + c);
+        double2 uu = *reinterpret_cast<const double2*>(a.f.u + c);
+        uu.x = fma(alpha, pp.x, uu.x);
+        uu.y = fma(alpha, pp.y, uu.y);
+        if (has_b)
+          *reinterpret_cast<double2*>(a.f.u + c) = uu;
+        else
+          a.f.u[c] = uu.x;
+      }
       rr.x = fma(-alpha, ww.x, rr.x);
       rr.y = fma(-alpha, ww.y, rr.y);
       double2 zz = rr;
@@ -230,11 +288,9 @@ __global__ void __launch_bounds__(FT) k_fused_cg_ur(LoopArgs a) {
         zz.y = mi.y * rr.y;
       }
       if (has_b) {
-        *reinterpret_cast<double2*>(a.f.u + c) = uu;
         *reinterpret_cast<double2*>(a.f.r + c) = rr;
         if (a.precond == 2) *reinterpret_cast<double2*>(a.f.z + c) = zz;
       } else {
-        a.f.u[c] = uu.x;
         a.f.r[c] = rr.x;
         if (a.precond == 2) a.f.z[c] = zz.x;
       }
@@ -326,6 +382,12 @@ void launch_fused_cg_ur(const LoopArgs& a, bool ppcg, cudaStream_t s) {
   } else {
     { ++launch_counter(); k_fused_cg_ur<UR_CG><<<grid, FT, 0, s>>>(a); }
   }
+}
+
+void launch_flush_u(const LoopArgs& a, cudaStream_t s) {
+  dim3 grid((a.L.nx + FT - 1) / FT, a.L.ny < 4096 ? a.L.ny : 4096);
+  { ++launch_counter(); k_flush_u<<<grid, FT, 0, s>>>(a); }
+  cudaMemsetAsync(&a.rd.st->u_pending, 0, sizeof(int), s);
 }
 
 }  // namespace tl

@@ -63,6 +63,8 @@ _IP = C.POINTER(C.c_int)
 SIGNATURES = {
     "tl_last_error": (C.c_char_p, []),
     "tl_set_device": (_I, [_I]),
+    "tl_host_register": (_I, [_P, C.c_ulonglong]),
+    "tl_host_unregister": (_I, [_P]),
     "tl_create": (_I, [_I, _I, _I, _I, _I, _I, _D, _D, C.POINTER(_P)]),
     "tl_destroy": (_I, [_P]),
     "tl_device_bytes": (_I, [_P, C.POINTER(C.c_ulonglong)]),
@@ -120,6 +122,25 @@ def load(build_if_missing: bool = True):
             fn.argtypes = args
         _lib = L
         return L
+
+
+class PinnedArray:
+    """A numpy array whose pages are registered with the driver (tl_host_register)."""
+
+    def __init__(self, shape, dtype=np.float64):
+        self.array = np.zeros(shape, dtype=dtype)
+        _check(load().tl_host_register(self.array.ctypes.data, self.array.nbytes))
+
+    def close(self):
+        if self.array is not None:
+            load().tl_host_unregister(self.array.ctypes.data)
+            self.array = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def set_device(device: int) -> None:
@@ -187,8 +208,12 @@ class Chunk:
             raise ValueError("expected shape (y_cells, x_cells)")
         _check(self.L.tl_upload_field(self.ptr, FIELD[field], _dp(a), self.nx))
 
-    def download(self, field: str) -> np.ndarray:
-        out = np.empty((self.ny, self.nx), dtype=np.float64)
+    def download(self, field: str, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """Interior of a field as (y_cells, x_cells); into ``out`` when given (C-contiguous float64)."""
+        if out is None:
+            out = np.empty((self.ny, self.nx), dtype=np.float64)
+        elif out.shape != (self.ny, self.nx) or out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 array of shape (y_cells, x_cells)")
         _check(self.L.tl_download_field(self.ptr, FIELD[field], _dp(out), self.nx))
         return out
 

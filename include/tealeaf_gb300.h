@@ -192,6 +192,20 @@ int tl_jacobi_solve(tl_ctx* ctx, double* error);
  * mask (bit f set for field id f, ids 1..11) when reflective_boundary; a no-op otherwise. */
 int tl_update_halo(tl_ctx* ctx, int field_mask, int depth);
 
+/* No counterpart in the reference.  tea_leaf_cg_calc_w_kernel (w = A p, pw = p.w) applied
+ * to device arrays the caller owns, laid out exactly as the reference's fields
+ * (1-h : x_cells+h, 1-h : y_cells+h, x fastest; Kx/Ky/Di as built by tea_leaf_common), for
+ * callers that cannot allocate device memory -- they manage every device buffer themselves
+ * (e.g. a Fortran driver keeping its fields on the GPU through OpenACC or CUDA Fortran), run
+ * under a fixed memory budget, or must not call cudaMalloc/cudaFree inside their time loop.
+ * Needs no tl_ctx and allocates nothing: the row sums of p.w use a fixed device array of
+ * 16384 + 32 doubles inside the library, so y_cells must be <= 16384 (larger sizes are
+ * rejected with TL_ERR_ARG).  The first call on each device, made with that device current,
+ * looks up the array's device address.  Runs on the default stream and returns after pw is
+ * on the host.  Calls that overlap on the GPU share the array and race. */
+int tl_cg_calc_w_noalloc(int x_cells, int y_cells, int halo_depth, const double* p, double* w, const double* kx,
+                         const double* ky, const double* di, double rx, double ry, double* pw);
+
 /* ---- whole solve -------------------------------------------------------- */
 
 /* tea_leaf() (tea_solve.f90:37-503) for one time step: initialisation, the CG /

@@ -40,6 +40,9 @@ enum Slot {
 
 }  // namespace
 
+// Lets the library's other translation units report through tl_last_error().
+void tl::set_last_error(const std::string& msg) { g_err = msg; }
+
 struct tl_ctx {
   int device = 0;
   Layout L{};

@@ -2,6 +2,8 @@
 // tl_kernels.cu, tl_fused.cu).  All launchers are asynchronous on the given stream.
 #pragma once
 
+#include <string>
+
 #include "tl_device.cuh"
 
 namespace tl {
@@ -17,6 +19,9 @@ constexpr int MAX_REDUCE_BLOCKS = 65536;
 
 // Number of kernels the launchers below have launched on the calling thread.
 long long& launch_counter();
+
+// Sets the message tl_last_error() returns on the calling thread.
+void set_last_error(const std::string& msg);
 
 // ---- set-up, summary, generation, halo ----------------------------------
 void launch_init_faces(const Fields& f, const Layout& L, const Geometry& g, cudaStream_t s);

@@ -94,6 +94,7 @@ SIGNATURES = {
     "tl_update_halo": (_I, [_P, _I, _I]),
     "tl_tea_leaf": (_I, [_P, C.POINTER(SolveOpts), _D, C.POINTER(SolveInfo)]),
     "tl_reset_eigen": (_I, [_P]),
+    "tl_cg_calc_w_noalloc": (_I, [_I, _I, _I, _P, _P, _P, _P, _P, _D, _D, _DP]),
     "tl_profile": (_I, [_P, _I]),
     "tl_profile_read": (_I, [_P, _I, _DP, C.POINTER(C.c_longlong)]),
 }

@@ -140,7 +140,7 @@ class Clocks:
             self.t.join(timeout=2)
 
     def summary(self):
-        sm, mx, reasons = [], [], set()
+        sm, mx, pw, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [x.strip() for x in ln.split(",")]
@@ -149,6 +149,7 @@ class Clocks:
             try:
                 sm.append(float(parts[1]))
                 mx.append(float(parts[2]))
+                pw.append(float(parts[3]))
             except ValueError:
                 continue
             for nm, v in zip(names, parts[5:9]):
@@ -157,7 +158,7 @@ class Clocks:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "power_w": statistics.median(pw) if pw else None}
 
 
 def cpu_port_steps(d, iters, steps, warmup, density=None, energy=None):
@@ -298,18 +299,31 @@ def main():
         chunk.tea_leaf(opts, dt)
         barrier()
         e_its = 0
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            chunk.upload_state(dens, ener)
-            info = chunk.tea_leaf(opts, dt)
-            e_its += min(info.n_exit, args.iters)
-            chunk.download("energy1", out=out)
-        e_wall = time.perf_counter() - t0
+        parts = [0.0, 0.0, 0.0, 0.0]  # upload, solve (host), solve (device), download
+        with Clocks(local) as clk_e2e:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                ta = time.perf_counter()
+                chunk.upload_state(dens, ener)
+                tb = time.perf_counter()
+                info = chunk.tea_leaf(opts, dt)
+                tc = time.perf_counter()
+                e_its += min(info.n_exit, args.iters)
+                chunk.download("energy1", out=out)
+                td = time.perf_counter()
+                parts[0] += tb - ta
+                parts[1] += tc - tb
+                parts[2] += info.solve_seconds
+                parts[3] += td - tc
+            e_wall = time.perf_counter() - t0
         barrier()
         e_wall = max_over_ranks(e_wall)
         e2e = {"value": world * cells * e_its / e_wall, "unit": "cell-iterations/s",
                "h2d_bytes_per_step": 2 * cells * 8, "d2h_bytes_per_step": cells * 8,
-               "ms_per_step": 1e3 * e_wall / args.steps}
+               "ms_per_step": 1e3 * e_wall / args.steps,
+               "ms_per_step_parts": {k: 1e3 * v / args.steps for k, v in
+                                     zip(("upload", "solve_host", "solve_device", "download"), parts)},
+               "clocks": clk_e2e.summary()}
 
     peak, peak_kind = measured_peaks()
     t_launch = mv_ms / mv_n * 1e-3 if mv_n else None

@@ -151,6 +151,7 @@ __global__ void __launch_bounds__(FT) k_fused_cg_w(LoopArgs a, int rows_per_cta)
   double* __restrict__ u = a.f.u;
 
   double acc[2] = {0.0, 0.0};
+  double acc_b = 0.0;  // second column's p.w chain, kept separate to shorten the FMA dependency chain
   double2 pm = make_double2(0.0, 0.0), pc = pm, pnx = pm, cyc = pm, oc = pm, onx = pm;
   if (active) {
     pc = pn_.pair(L.at(ja, k0), oc);
@@ -194,7 +195,7 @@ __global__ void __launch_bounds__(FT) k_fused_cg_w(LoopArgs a, int rows_per_cta)
         wb = fma(-cyc.y, pm.y, wb);
         wb = fma(-cxr, right_b, wb);
         wb = fma(-cxa.y, pc.x, wb);
-        acc[0] = fma(wb, pc.y, acc[0]);
+        acc_b = fma(wb, pc.y, acc_b);
         *reinterpret_cast<double2*>(w + c) = make_double2(wa, wb);
         *reinterpret_cast<double2*>(pout + c) = pc;
         if (upd_u) {
@@ -225,6 +226,7 @@ __global__ void __launch_bounds__(FT) k_fused_cg_w(LoopArgs a, int rows_per_cta)
     pc = pnx;
     oc = onx;
   }
+  acc[0] += acc_b;
   grid_reduce<2>(acc, a.rd, EpiCgW{a.rd, PPCG});
 }
 
@@ -353,7 +355,9 @@ inline int strips(const Layout& L) { return (L.nx + SW - 1) / SW; }
 
 void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s) {
   const int ns = strips(a.L);
-  // aim for >= ~8 CTAs per SM of 152, with 8..64 rows per CTA
+  // 8..64 rows per CTA, aiming at >= ~8 CTAs per SM of 152.  Measured at 8192^2: 64-row
+  // CTAs over three waves (1.031 ms) beat one resident wave of ~196-row CTAs (1.055 ms),
+  // although the latter recomputes fewer edge rows.
   int rows = (int)(((long long)a.L.ny * ns) / (152 * 8));
   rows = rows < 8 ? 8 : (rows > 64 ? 64 : rows);
   const int min_rows = (int)(((long long)a.L.ny * ns + MAX_REDUCE_BLOCKS - 1) / MAX_REDUCE_BLOCKS);

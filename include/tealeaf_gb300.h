@@ -82,7 +82,17 @@ typedef struct tl_solve_opts {
   double ch_cg_epslim;   /* tl_ch_cg_epslim */
   int ppcg_inner_steps;  /* tl_ppcg_inner_steps (after the PPCG default) */
   int check_result;      /* tl_check_result */
+  /* Precision form (no reference counterpart): TL_PRECISION_FP64 runs the reference's
+   * algorithm in FP64; TL_PRECISION_MIXED (CG only) runs FP32 inner CG solves on FP32
+   * copies of the operator inside FP64 iterative refinement: FP64 true residual u0 - A u,
+   * FP64 reductions and step coefficients, u updated in FP64. */
+  int precision;
+  double inner_tol;      /* mixed: relative residual reduction of each inner solve (0: 1e-4) */
+  int max_inner_iters;   /* mixed: cap on one inner solve (0: max_iters) */
 } tl_solve_opts;
+
+#define TL_PRECISION_FP64 0
+#define TL_PRECISION_MIXED 1
 
 /* Outcome of one solve (the lines tea_solve.f90:435-456 prints, plus counters). */
 typedef struct tl_solve_info {
@@ -98,6 +108,9 @@ typedef struct tl_solve_info {
   double eigmin, eigmax;
   double solve_seconds;     /* device time of the whole call (CUDA events on its stream) */
   long long kernel_launches; /* kernels this call launched */
+  int outer_iterations;     /* mixed: refinement steps (0 for the FP64 form) */
+  int pad_;
+  double true_residual;     /* mixed: final sqrt(|u0 - A u|^2) computed in FP64 */
 } tl_solve_info;
 
 /* Kernel ids for the per-kernel timers (tl_profile_read). */

@@ -78,6 +78,11 @@ struct tl_ctx {
   double prof_ms[TL_NUM_KERNEL_TIMERS] = {};
   long long prof_n[TL_NUM_KERNEL_TIMERS] = {};
   long long nlaunch = 0;  // kernels launched by the current tl_tea_leaf call
+  // mixed-precision form: FP32 fields (allocated on first use) and the inner-loop state
+  char* mix_slab = nullptr;
+  MixFields mix{};
+  MixState* mst = nullptr;
+  MixState* mst_host = nullptr;
 
   double* slot(int s) const { return reinterpret_cast<double*>(slab + (size_t)s * field_stride); }
   Reduce rd() const { return Reduce{partials, counter, st, hist_a, hist_b, ch_a, ch_b}; }
@@ -364,6 +369,9 @@ int tl_destroy(tl_ctx* c) {
   cudaFree(c->ch_b);
   cudaFree(c->states_dev);
   cudaFree(c->halo_list);
+  cudaFree(c->mix_slab);
+  cudaFree(c->mst);
+  if (c->mst_host) cudaFreeHost(c->mst_host);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   for (int i = 0; i < 3 * tl_ctx::BATCH; ++i)
@@ -692,6 +700,85 @@ int tl_profile_read(tl_ctx* c, int kernel_id, double* total_ms, long long* launc
 // ===========================================================================
 namespace {
 
+int ensure_mix(tl_ctx* c) {
+  if (c->mix_slab) return TL_OK;
+  const size_t fb = ((size_t)c->L.elems() * sizeof(float) + 4 * 256 + 255) / 256 * 256;
+  CK(cudaMalloc(&c->mix_slab, fb * 8));
+  CK(cudaMemsetAsync(c->mix_slab, 0, fb * 8, c->stream));
+  float* b = reinterpret_cast<float*>(c->mix_slab);
+  const size_t step = fb / sizeof(float);
+  c->mix = MixFields{b, b + step, b + 2 * step, b + 3 * step, b + 4 * step, b + 5 * step, b + 6 * step, b + 7 * step};
+  CK(cudaMalloc(&c->mst, sizeof(MixState)));
+  CK(cudaMallocHost(&c->mst_host, sizeof(MixState)));
+  return TL_OK;
+}
+
+int sync_mix(tl_ctx* c) {
+  CK(cudaMemcpyAsync(c->mst_host, c->mst, sizeof(MixState), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+// Mixed-precision CG (tl_mixed.cu): FP64 refinement loop around FP32 inner CG solves.
+// Called by tl_tea_leaf after the set-up kernels; finishes the solve (finalise included).
+int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long launches0) {
+  int rc;
+  if ((rc = ensure_mix(c))) return rc;
+  MixState& H = *c->mst_host;
+  memset(&H, 0, sizeof(H));
+  H.inner_tol = o->inner_tol > 0.0 ? o->inner_tol : 1e-4;
+  H.max_n = o->max_inner_iters > 0 ? o->max_inner_iters : o->max_iters;
+  CK(cudaMemcpyAsync(c->mst, &H, sizeof(MixState), cudaMemcpyHostToDevice, c->stream));
+  launch_mix_prep(c->f, c->mix, c->L, c->stream);
+  const Reduce rd = c->rd();
+  launch_mix_residual(c->f, c->mix, c->L, rd, c->mst, c->stream);
+  if ((rc = check_launch("mixed set-up"))) return rc;
+  if ((rc = sync_mix(c))) return rc;
+  const double initial_residual = std::sqrt(std::fabs(H.outer_rr));
+  double res = initial_residual, prev = initial_residual;
+  int outer = 0, inner_total = 0;
+  const int batch = tl_ctx::BATCH;
+  while (res >= o->eps * initial_residual && inner_total < o->max_iters) {
+    // inner FP32 CG on A d = r
+    while (H.status == RUN) {
+      for (int i = 0; i < batch; ++i) launch_mix_iteration(c->mix, c->L, rd, c->mst, c->stream);
+      if ((rc = check_launch("mixed inner batch"))) return rc;
+      if ((rc = sync_mix(c))) return rc;
+    }
+    if (H.status == EXIT_BREAKDOWN) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite inner CG scalar");
+    inner_total += H.n;
+    ++outer;
+    launch_mix_apply(c->f, c->mix, c->L, c->mst, c->stream);  // u += d (FP64)
+    if ((rc = do_halo(c, M(TL_FIELD_U), 1))) return rc;
+    launch_mix_residual(c->f, c->mix, c->L, rd, c->mst, c->stream);
+    if ((rc = check_launch("mixed refinement"))) return rc;
+    if ((rc = sync_mix(c))) return rc;
+    res = std::sqrt(std::fabs(H.outer_rr));
+    if (!std::isfinite(res)) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite residual");
+    // at the FP64 accuracy floor of u0 - A u the true residual stops falling
+    if (res > 0.5 * prev) break;
+    prev = res;
+  }
+  launch_finalise(c->f, c->L, c->stream);
+  if ((rc = do_halo(c, M(TL_FIELD_ENERGY1), 1))) return rc;
+  if ((rc = check_launch("finalise"))) return rc;
+  CK(cudaEventRecord(c->ev1, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  info->n_exit = inner_total;
+  info->reported_iterations = inner_total;
+  info->cg_calc_steps = inner_total;
+  info->initial_residual = initial_residual;
+  info->error = res;
+  info->exact_error = res;
+  info->true_residual = res;
+  info->outer_iterations = outer;
+  info->solve_seconds = ms * 1e-3;
+  info->kernel_launches = launch_counter() - launches0;
+  return TL_OK;
+}
+
 struct Solver {
   tl_ctx* c;
   const tl_solve_opts* o;
@@ -732,6 +819,10 @@ extern "C" int tl_tea_leaf(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solv
   if (!c || !o || !info) return fail(TL_ERR_ARG, "tl_tea_leaf: null argument");
   if (o->solver < TL_SOLVER_JACOBI || o->solver > TL_SOLVER_PPCG) return fail(TL_ERR_ARG, "tl_tea_leaf: bad solver");
   if (o->max_iters < 1) return fail(TL_ERR_ARG, "tl_tea_leaf: max_iters must be >= 1");
+  if (o->precision != TL_PRECISION_FP64 && o->precision != TL_PRECISION_MIXED)
+    return fail(TL_ERR_ARG, "tl_tea_leaf: unknown precision form");
+  if (o->precision == TL_PRECISION_MIXED && (o->solver != TL_SOLVER_CG || c->g.precond != TL_PREC_NONE))
+    return fail(TL_ERR_ARG, "tl_tea_leaf: the mixed-precision form is implemented for unpreconditioned CG");
   memset(info, 0, sizeof(*info));
   Solver S{c, o, o->solver == TL_SOLVER_CG, o->solver == TL_SOLVER_CHEBY, o->solver == TL_SOLVER_PPCG,
            o->solver == TL_SOLVER_JACOBI, {}, {}};
@@ -750,6 +841,7 @@ extern "C" int tl_tea_leaf(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solv
   launch_init_faces(c->f, c->L, c->g, c->stream);
   launch_init_cells(c->f, c->L, c->g, false, c->stream);
   if ((rc = do_halo(c, M(TL_FIELD_U), 1))) return rc;
+  if (o->precision == TL_PRECISION_MIXED) return mixed_cg(c, o, info, launches0);
   LoopState& H = *c->st_host;
   memset(&H, 0, sizeof(H));
   H.eps = o->eps;

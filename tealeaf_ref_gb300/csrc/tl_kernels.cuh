@@ -81,4 +81,21 @@ void launch_fused_ppcg_inner(const LoopArgs& a, const double* sd_in, double* sd_
 void launch_fused_jacobi(const LoopArgs& a, const double* un, double* u_out, cudaStream_t s);
 void launch_jacobi_denominator(const Fields& f, const Layout& L, const Geometry& g, cudaStream_t s);
 
+// ---- mixed precision: FP32 inner CG inside FP64 iterative refinement (tl_mixed.cu) ----
+struct MixFields {
+  float *cx, *cy, *di;  // FP32 copies of the pre-scaled operator
+  float *r, *p, *p2, *w, *d;
+};
+struct MixState {
+  double rro, pw, rr, rr0, tol2, alpha, beta;  // inner CG scalars (FP64)
+  double outer_rr;                             // ||u0 - A u||^2 in FP64
+  double d_alpha, inner_tol;
+  int n, max_n, status, p_pending, d_pending, d_psel;
+};
+void launch_mix_prep(const Fields& f, const MixFields& m, const Layout& L, cudaStream_t s);
+void launch_mix_residual(const Fields& f, const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms,
+                         cudaStream_t s);
+void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms, cudaStream_t s);
+void launch_mix_apply(const Fields& f, const MixFields& m, const Layout& L, MixState* ms, cudaStream_t s);
+
 }  // namespace tl

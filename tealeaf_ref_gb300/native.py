@@ -34,9 +34,13 @@ class TeaLeafError(RuntimeError):
         self.code = code
 
 
+PRECISION = {"fp64": 0, "mixed": 1}
+
+
 class SolveOpts(C.Structure):
     _fields_ = [("solver", C.c_int), ("max_iters", C.c_int), ("eps", C.c_double), ("ch_cg_presteps", C.c_int),
-                ("ch_cg_epslim", C.c_double), ("ppcg_inner_steps", C.c_int), ("check_result", C.c_int)]
+                ("ch_cg_epslim", C.c_double), ("ppcg_inner_steps", C.c_int), ("check_result", C.c_int),
+                ("precision", C.c_int), ("inner_tol", C.c_double), ("max_inner_iters", C.c_int)]
 
 
 class SolveInfo(C.Structure):
@@ -44,7 +48,8 @@ class SolveInfo(C.Structure):
                 ("cg_calc_steps", C.c_int), ("cheby_calc_steps", C.c_int), ("est_itc", C.c_int),
                 ("initial_residual", C.c_double), ("error", C.c_double), ("exact_error", C.c_double),
                 ("eigmin", C.c_double), ("eigmax", C.c_double), ("solve_seconds", C.c_double),
-                ("kernel_launches", C.c_longlong)]
+                ("kernel_launches", C.c_longlong), ("outer_iterations", C.c_int), ("pad_", C.c_int),
+                ("true_residual", C.c_double)]
 
     def as_dict(self):
         return {f[0]: getattr(self, f[0]) for f in self._fields_}
@@ -158,10 +163,14 @@ def _dp(a: np.ndarray):
     return a.ctypes.data_as(_DP)
 
 
-def opts_from_deck(deck: Deck) -> SolveOpts:
+def opts_from_deck(deck: Deck, precision: str = "fp64", inner_tol: float = 0.0,
+                   max_inner_iters: int = 0) -> SolveOpts:
+    """Solve options from a deck; ``precision`` "mixed" selects FP32 inner CG solves inside
+    FP64 iterative refinement (CG without preconditioner)."""
     return SolveOpts(solver=deck.solver_id, max_iters=deck.max_iters, eps=deck.eps, ch_cg_presteps=deck.ch_cg_presteps,
                      ch_cg_epslim=deck.ch_cg_epslim, ppcg_inner_steps=deck.effective_inner_steps(),
-                     check_result=int(deck.check_result))
+                     check_result=int(deck.check_result), precision=PRECISION[precision], inner_tol=inner_tol,
+                     max_inner_iters=max_inner_iters)
 
 
 class Chunk:
@@ -337,9 +346,10 @@ class RunResult:
     solves: List[dict]
 
 
-def run_deck(deck: Deck, max_steps: Optional[int] = None) -> RunResult:
+def run_deck(deck: Deck, max_steps: Optional[int] = None, precision: str = "fp64", inner_tol: float = 0.0) -> RunResult:
     """The reference's main program on one GPU chunk: start (generate, set_field, first
     field_summary; start.f90:98-125) then the diffuse loop (diffuse.f90:43-105)."""
+    opts = opts_from_deck(deck, precision, inner_tol)
     with Chunk.from_deck(deck) as c:
         summaries = [(0, c.field_summary())]
         solves = []
@@ -348,7 +358,7 @@ def run_deck(deck: Deck, max_steps: Optional[int] = None) -> RunResult:
         while True:
             step += 1
             dt = deck.initial_timestep
-            solves.append(c.tea_leaf(deck, dt).as_dict())
+            solves.append(c.tea_leaf(opts, dt).as_dict())
             time = time + dt
             done = time + g_small > deck.end_time or step >= deck.end_step or bool(max_steps and step >= max_steps)
             if deck.summary_frequency and step % deck.summary_frequency == 0 and not done:

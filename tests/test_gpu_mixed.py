@@ -1,0 +1,69 @@
+"""The mixed-precision form (FP32 inner CG inside FP64 iterative refinement) against the
+FP64 oracle: the same field-summary (1e-10) and per-cell u (1e-8) bars as the FP64 form."""
+import numpy as np
+import pytest
+
+from helpers import small_deck
+from tealeaf_ref_gb300 import deck as dk
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.max(np.abs(a - b) / np.abs(b)))
+
+
+CASES = [
+    dict(),
+    dict(coefficient=1),
+    dict(reflective=True),
+    dict(nx=200, ny=131, n_rect=6, n_circ=3),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=["-".join("%s%s" % kv for kv in c.items()) or "default" for c in CASES])
+def test_mixed_cg_matches_fp64_oracle(case):
+    from oracle import oracle
+    from tealeaf_ref_gb300 import native
+
+    kw = dict(nx=67, ny=45, steps=3, n_rect=4, n_circ=2, max_iters=20000)
+    kw.update(case)
+    d = small_deck(**kw)
+    ro = oracle.run_deck(d)
+    opts = native.opts_from_deck(d, precision="mixed")
+    with native.Chunk.from_deck(d) as c:
+        infos = [c.tea_leaf(opts, d.initial_timestep) for _ in range(d.end_step)]
+        s = c.field_summary()
+        u = c.download("u")
+    o = oracle.Chunk.from_deck(d)
+    for _ in range(d.end_step):
+        o.tea_leaf(d)
+    assert _rel(s, ro.summaries[-1][1]) < 1e-10
+    assert _rel(u, np.array(o.interior("u"))) < 1e-8
+    for i in infos:
+        assert i.outer_iterations >= 1
+        assert i.true_residual <= 1e-9 * i.initial_residual
+
+
+def test_mixed_cg_reference_deck(golden):
+    """tea_bm_2 (250^2, default coefficient) in the mixed form against the reference's output."""
+    from tealeaf_ref_gb300 import native
+
+    g = golden["benchmarks"]["tea_bm_2"]
+    d = dk.parse_deck(g["deck"])
+    res = native.run_deck(d, precision="mixed")
+    s = res.summaries[-1][1]
+    want = g["summaries"][-1]
+    ref = [want["volume"], want["mass"], want["energy"], want["temperature"]]
+    assert _rel(s, ref) < 1e-10
+
+
+def test_mixed_rejected_for_other_solvers():
+    from tealeaf_ref_gb300 import native
+
+    d = small_deck(nx=16, ny=16, solver="ppcg", ppcg_inner_steps=4)
+    with native.Chunk.from_deck(d) as c:
+        with pytest.raises(native.TeaLeafError) as e:
+            c.tea_leaf(native.opts_from_deck(d, precision="mixed"), d.initial_timestep)
+        assert e.value.code == -1

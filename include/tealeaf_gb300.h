@@ -83,12 +83,14 @@ typedef struct tl_solve_opts {
   int ppcg_inner_steps;  /* tl_ppcg_inner_steps (after the PPCG default) */
   int check_result;      /* tl_check_result */
   /* Precision form (no reference counterpart): TL_PRECISION_FP64 runs the reference's
-   * algorithm in FP64; TL_PRECISION_MIXED (CG only) runs FP32 inner CG solves on FP32
-   * copies of the operator inside FP64 iterative refinement: FP64 true residual u0 - A u,
-   * FP64 reductions and step coefficients, u updated in FP64. */
+   * algorithm in FP64; TL_PRECISION_MIXED (unpreconditioned CG) runs CG on FP32 vectors and
+   * FP32 copies of the operator, with FP64 reductions and step coefficients, the solution
+   * accumulated in FP64 and the residual periodically replaced by the FP64 true residual
+   * u0 - A u (the CG search direction is kept across replacements). */
   int precision;
-  double inner_tol;      /* mixed: relative residual reduction of each inner solve (0: 1e-4) */
-  int max_inner_iters;   /* mixed: cap on one inner solve (0: max_iters) */
+  double inner_tol;      /* mixed: replace the residual each time it has fallen by this
+                            factor since the last replacement (0: 0.1) */
+  int max_inner_iters;   /* mixed: cap on FP32 CG steps (0: max_iters) */
 } tl_solve_opts;
 
 #define TL_PRECISION_FP64 0

@@ -294,7 +294,9 @@ int tl_create(int x_cells, int y_cells, int halo_depth, int coefficient, int pre
   c->halo_depth = halo_depth;
   c->L.nx = x_cells;
   c->L.ny = y_cells;
-  c->L.ld = ((XOFF + x_cells + 2 + 15) / 16) * 16;
+  // room after the right halo cell for a 4-wide (FP32) or 2-wide (FP64) vector load that starts
+  // at the last interior column
+  c->L.ld = ((XOFF + x_cells + 4 + 15) / 16) * 16;
   c->g.dx = dx;
   c->g.dy = dy;
   c->g.coefficient = coefficient;
@@ -726,39 +728,63 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
   if ((rc = ensure_mix(c))) return rc;
   MixState& H = *c->mst_host;
   memset(&H, 0, sizeof(H));
-  H.inner_tol = o->inner_tol > 0.0 ? o->inner_tol : 1e-4;
-  H.max_n = o->max_inner_iters > 0 ? o->max_inner_iters : o->max_iters;
+  const double delta = o->inner_tol > 0.0 ? o->inner_tol : 0.1;
+  H.delta2 = delta * delta;
+  H.max_n = o->max_inner_iters > 0 ? std::min(o->max_inner_iters, o->max_iters) : o->max_iters;
+  H.phase_end = 0x7fffffff;
+  const Reduce rd = c->rd();
+  const size_t fbytes = (size_t)c->L.elems() * sizeof(float);
+  CK(cudaMemsetAsync(c->mix.d, 0, fbytes, c->stream));  // a rejected correction may remain
   CK(cudaMemcpyAsync(c->mst, &H, sizeof(MixState), cudaMemcpyHostToDevice, c->stream));
   launch_mix_prep(c->f, c->mix, c->L, c->stream);
-  const Reduce rd = c->rd();
-  launch_mix_residual(c->f, c->mix, c->L, rd, c->mst, c->stream);
+  launch_mix_trial(c->f, c->mix, c->L, rd, c->mst, true, c->stream);  // r = p = u0 - A u
   if ((rc = check_launch("mixed set-up"))) return rc;
   if ((rc = sync_mix(c))) return rc;
-  const double initial_residual = std::sqrt(std::fabs(H.outer_rr));
+  const double initial_residual = std::sqrt(std::fabs(H.trial_rr));
+  H.rro = H.rr = H.rr_max = H.trial_rr32;
+  H.n = 1;
+  H.p_pending = 0;
+  H.d_pending = 0;
+  H.status = (H.trial_rr32 > 0.0 && std::isfinite(H.trial_rr32)) ? RUN : EXIT_CONVERGED;
   double res = initial_residual, prev = initial_residual;
-  int outer = 0, inner_total = 0;
+  int outer = 0, last_phase = 0;
   const int batch = tl_ctx::BATCH;
-  while (res >= o->eps * initial_residual && inner_total < o->max_iters) {
-    // inner FP32 CG on A d = r
+  while (res >= o->eps * initial_residual && H.status == RUN) {
+    // FP32 CG steps until the recursive residual has fallen by delta since the last
+    // replacement; after the first phase each phase gets a step budget, so a process that
+    // has lost its way near the accuracy floor is stopped and checked
+    H.phase_end = last_phase > 0 ? H.n + std::max(64, 4 * last_phase) : 0x7fffffff;
+    CK(cudaMemcpyAsync(c->mst, &H, sizeof(MixState), cudaMemcpyHostToDevice, c->stream));
+    const int n_start = H.n;
     while (H.status == RUN) {
       for (int i = 0; i < batch; ++i) launch_mix_iteration(c->mix, c->L, rd, c->mst, c->stream);
-      if ((rc = check_launch("mixed inner batch"))) return rc;
+      if ((rc = check_launch("mixed batch"))) return rc;
       if ((rc = sync_mix(c))) return rc;
     }
-    if (H.status == EXIT_BREAKDOWN) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite inner CG scalar");
-    inner_total += H.n;
-    ++outer;
-    launch_mix_apply(c->f, c->mix, c->L, c->mst, c->stream);  // u += d (FP64)
-    if ((rc = do_halo(c, M(TL_FIELD_U), 1))) return rc;
-    launch_mix_residual(c->f, c->mix, c->L, rd, c->mst, c->stream);
-    if ((rc = check_launch("mixed refinement"))) return rc;
+    if (H.status == EXIT_BREAKDOWN) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite FP32 CG scalar");
+    last_phase = H.n - n_start;
+    const bool capped = H.n > H.max_n;
+    // trial replacement: true FP64 residual of u + d, u itself untouched
+    launch_mix_flush_d(c->mix, c->L, c->mst, c->stream);  // the trial's epilogue clears d_pending
+    launch_mix_trial(c->f, c->mix, c->L, rd, c->mst, false, c->stream);
+    if ((rc = check_launch("mixed trial residual"))) return rc;
     if ((rc = sync_mix(c))) return rc;
-    res = std::sqrt(std::fabs(H.outer_rr));
-    if (!std::isfinite(res)) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite residual");
+    const double res_t = std::sqrt(std::fabs(H.trial_rr));
+    if (!std::isfinite(res_t)) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite residual");
+    if (!(res_t < prev)) break;  // no gain: keep u, drop the correction
+    launch_mix_apply(c->f, c->mix, c->L, c->stream);  // accept: u += d, d = 0
+    ++outer;
+    res = res_t;
     // at the FP64 accuracy floor of u0 - A u the true residual stops falling
-    if (res > 0.5 * prev) break;
+    if (capped || res > 0.5 * prev) break;
     prev = res;
+    // continue the CG process with r replaced by the true residual, search direction kept
+    H.beta = H.trial_rr32 / H.rro_prev;
+    H.rro = H.rr = H.rr_max = H.trial_rr32;
+    H.p_pending = 1;
+    H.status = RUN;
   }
+  const int inner_total = H.n - 1;
   launch_finalise(c->f, c->L, c->stream);
   if ((rc = do_halo(c, M(TL_FIELD_ENERGY1), 1))) return rc;
   if ((rc = check_launch("finalise"))) return rc;

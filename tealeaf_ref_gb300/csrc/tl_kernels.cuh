@@ -87,15 +87,22 @@ struct MixFields {
   float *r, *p, *p2, *w, *d;
 };
 struct MixState {
-  double rro, pw, rr, rr0, tol2, alpha, beta;  // inner CG scalars (FP64)
-  double outer_rr;                             // ||u0 - A u||^2 in FP64
-  double d_alpha, inner_tol;
-  int n, max_n, status, p_pending, d_pending, d_psel;
+  double rro, rro_prev, pw, rr, alpha, beta;  // FP32-vector CG scalars (FP64)
+  double rr_max;                              // r.r at the last residual replacement
+  double delta2;                              // replace when r.r < delta2 * rr_max
+  double trial_rr;                            // ||u0 - A (u + d)||^2 in FP64 (last trial)
+  double trial_rr32;                          // r.r of its FP32 rounding
+  double d_alpha;
+  int n, max_n, phase_end, status, p_pending, d_pending, d_psel;
 };
 void launch_mix_prep(const Fields& f, const MixFields& m, const Layout& L, cudaStream_t s);
-void launch_mix_residual(const Fields& f, const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms,
-                         cudaStream_t s);
+// d += alpha p if an update is pending (the host clears MixState::d_pending afterwards)
+void launch_mix_flush_d(const MixFields& m, const Layout& L, MixState* ms, cudaStream_t s);
+// trial residual r = u0 - A (u + d) in FP64 (u unchanged), r32 = r; first: also p32 = r
+void launch_mix_trial(const Fields& f, const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms,
+                      bool first, cudaStream_t s);
 void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms, cudaStream_t s);
-void launch_mix_apply(const Fields& f, const MixFields& m, const Layout& L, MixState* ms, cudaStream_t s);
+// accept the correction: u += d (FP64), d = 0
+void launch_mix_apply(const Fields& f, const MixFields& m, const Layout& L, cudaStream_t s);
 
 }  // namespace tl

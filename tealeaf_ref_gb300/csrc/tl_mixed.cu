@@ -1,13 +1,20 @@
-// tl_mixed.cu -- the mixed-precision form of the CG solve: FP32 inner CG on FP32 copies of
-// the operator, wrapped in FP64 iterative refinement.
+// tl_mixed.cu -- the mixed-precision form of the CG solve: CG on FP32 vectors and FP32
+// copies of the operator, with the solution accumulated and the residual periodically
+// recomputed in FP64 ("reliable updates": van der Vorst & Ye, SIAM J. Sci. Comput. 22,
+// 2000; Clark et al., Comput. Phys. Commun. 181, 2010).
 //
-// Outer loop (FP64): r = u0 - A u (true residual, tea_leaf_common_kernel.f90:208-244
-// arithmetic in FP64), ||r||^2 in FP64; stop when sqrt(||r||^2) < eps * initial residual
-// (the reference's test, tea_solve.f90:410) or when the true residual no longer falls (the
-// FP64 accuracy floor of b - A u).  Inner loop (FP32 vectors): CG on A d = r, d0 = 0, to a
-// relative reduction `inner_tol` of its recursively updated residual; then u += d in FP64.
+// The FP32 CG process runs on the correction d (u = u_64 + d).  When its recursively
+// updated residual has fallen by `delta` (tl_solve_opts.inner_tol) since the last
+// replacement, or a phase has used its step budget, the true residual of u + d is computed
+// in FP64 (tea_leaf_common_kernel.f90:208-244 arithmetic) without touching u.  If it is
+// lower than the last accepted one, the correction is folded into u in FP64, the true
+// residual replaces the FP32 residual and the CG process continues with its search
+// direction kept -- unlike a restarted refinement, the Krylov process is not thrown away.
+// Otherwise the correction is dropped and u stays the best iterate.  The solve stops when the
+// true residual satisfies the reference's test sqrt(r.r) < eps * initial residual
+// (tea_solve.f90:410) or stops falling (the FP64 accuracy floor of u0 - A u).
 //
-// The inner sweeps are the FP64 fused CG sweeps (tl_fused.cu) on float data: p update +
+// The FP32 sweeps are the FP64 fused CG sweeps (tl_fused.cu) on float data: p update +
 // 5-point matvec + p.w with the deferred d += alpha p, and r -= alpha w + r.r.  They move 48
 // bytes per cell-iteration and do no FP64 arithmetic per cell: the dot products are summed
 // per thread with the compensated FP32 algorithm Dot2 (TwoProduct via FMA + TwoSum; Ogita,
@@ -23,8 +30,8 @@ namespace tl {
 
 namespace {
 
-constexpr int MT = 128;     // threads per CTA
-constexpr int MSW = 2 * MT; // strip width
+constexpr int MT = 128;      // threads per CTA
+constexpr int MSW = 4 * MT;  // strip width (four columns per thread)
 
 // ---- error-free transformations (Knuth's TwoSum; TwoProduct with FMA) ----
 struct Dot2 {
@@ -42,28 +49,24 @@ struct Dot2 {
 };
 
 __device__ __forceinline__ void mix_finish(MixState* ms) {
-  // inner CG convergence on its recursively updated residual, or the iteration cap
-  if (!(ms->rr > ms->tol2) || ms->n >= ms->max_n) {
+  ms->n += 1;
+  // hand over to the host for a residual replacement (the recursive residual fell by delta,
+  // or this phase used up its step budget), or stop at the overall cap
+  if (!(ms->rr > ms->delta2 * ms->rr_max) || ms->n > ms->max_n || ms->n >= ms->phase_end)
     ms->status = EXIT_CONVERGED;
-  } else {
-    ms->n += 1;
-  }
 }
 
-struct EpiMixResidual {
+// Records the norms of a trial residual; the host decides whether to accept the correction.
+// The pending d update was flushed before the trial (k_mix_flush_d), so it is cleared here.
+struct EpiMixTrial {
   MixState* ms;
   __device__ void operator()(double (&acc)[2]) const {
-    ms->outer_rr = acc[0];
-    ms->rro = acc[1];
-    ms->rr0 = acc[1];
-    ms->rr = acc[1];
-    ms->tol2 = ms->inner_tol * ms->inner_tol * acc[1];
-    ms->n = 1;
-    ms->status = (acc[1] > 0.0 && isfinite(acc[1])) ? RUN : EXIT_CONVERGED;
-    ms->p_pending = 0;
+    ms->trial_rr = acc[0];
+    ms->trial_rr32 = acc[1];
     ms->d_pending = 0;
   }
 };
+
 
 struct EpiMixW {
   MixState* ms;
@@ -81,6 +84,7 @@ struct EpiMixUr {
   __device__ void operator()(double (&acc)[1]) const {
     ms->rr = acc[0];
     ms->beta = acc[0] / ms->rro;
+    ms->rro_prev = ms->rro;
     ms->rro = acc[0];
     ms->p_pending = 1;
     ms->d_pending = 1;
@@ -106,31 +110,55 @@ __global__ void k_mix_prep(Fields f, MixFields m, Layout L) {
   }
 }
 
-// Outer residual in FP64: r = u0 - A u; ||r||^2 (FP64) and the inner start r32 = p32 = r,
-// ||r32||^2, d32 = 0.
-__global__ void k_mix_residual(Fields f, MixFields m, Layout L, Reduce rd, MixState* ms) {
+// Trial residual in FP64 of the corrected solution: r = u0 - A (u + d), with off-domain
+// neighbours mirrored (the reflective halo copy, or a value multiplied by a zero boundary
+// coefficient), so u's halo is not needed.  r32 = r; ||r||^2 and ||r32||^2 in FP64.
+// first: the start of the CG process, p32 = r32.
+__global__ void k_mix_trial(Fields f, MixFields m, Layout L, Reduce rd, MixState* ms, bool first) {
   double acc[2] = {0.0, 0.0};
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
     if (j > L.nx) continue;
     const long long c = L.at(j, k);
-    double a = f.di[c] * f.u[c];
-    a = fma(-f.cy[c + L.ld], f.u[c + L.ld], a);
-    a = fma(-f.cy[c], f.u[c - L.ld], a);
-    a = fma(-f.cx[c + 1], f.u[c + 1], a);
-    a = fma(-f.cx[c], f.u[c - 1], a);
+    const long long cl = (j > 1) ? c - 1 : c, cr = (j < L.nx) ? c + 1 : c;
+    const long long cb = (k > 1) ? c - L.ld : c, ct = (k < L.ny) ? c + L.ld : c;
+    const double uc = f.u[c] + (double)m.d[c];
+    const double ul = f.u[cl] + (double)m.d[cl], ur = f.u[cr] + (double)m.d[cr];
+    const double ub = f.u[cb] + (double)m.d[cb], ut = f.u[ct] + (double)m.d[ct];
+    double a = f.di[c] * uc;
+    a = fma(-f.cy[c + L.ld], ut, a);
+    a = fma(-f.cy[c], ub, a);
+    a = fma(-f.cx[c + 1], ur, a);
+    a = fma(-f.cx[c], ul, a);
     const double r = f.u0[c] - a;
     acc[0] = fma(r, r, acc[0]);
     const float r32 = (float)r;
     m.r[c] = r32;
-    m.p[c] = r32;
-    m.d[c] = 0.f;
+    if (first) m.p[c] = r32;
     acc[1] = fma((double)r32, (double)r32, acc[1]);
   }
-  grid_reduce<2>(acc, rd, EpiMixResidual{ms});
+  grid_reduce<2>(acc, rd, EpiMixTrial{ms});
 }
 
+
+// Four adjacent columns (ja .. ja+3) per thread: 16-byte loads of every FP32 stream.
+struct F4 {
+  float v[4];
+  __device__ __forceinline__ void load(const float* __restrict__ p, long long c) {
+    const float4 q = *reinterpret_cast<const float4*>(p + c);
+    v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+  }
+  __device__ __forceinline__ void store(float* __restrict__ p, long long c, int nv) const {
+    if (nv == 4) {
+      *reinterpret_cast<float4*>(p + c) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+      for (int i = 0; i < nv; ++i) p[c + i] = v[i];
+    }
+  }
+};
+
 // p_n = r + beta p_{n-1} (FP32), w = A p_n (FP32), p.w (Dot2), deferred d += alpha p_{n-1}.
+// Same row march as the FP64 sweep (tl_fused.cu), four columns per thread.
 __global__ void __launch_bounds__(MT) k_mix_w(MixFields m, Layout L, Reduce rd, MixState* ms, int rows_per_cta) {
   if (ms->status != RUN) return;
   const int n = ms->n;
@@ -144,72 +172,76 @@ __global__ void __launch_bounds__(MT) k_mix_w(MixFields m, Layout L, Reduce rd, 
   __shared__ float buf[2][MSW + 2];
   const int t = threadIdx.x;
   const int js = blockIdx.x * MSW + 1;
-  const int ja = js + 2 * t;
-  const bool active = ja <= L.nx, has_b = ja + 1 <= L.nx;
+  const int ja = js + 4 * t;
+  const int nv = min(4, L.nx - ja + 1);  // interior columns this thread owns
+  const bool active = nv > 0;
   const int k0 = blockIdx.y * rows_per_cta + 1;
   const int k1 = min(k0 + rows_per_cta - 1, L.ny);
-  auto pnew = [&](long long c, float2& old) {
-    old = *reinterpret_cast<const float2*>(pold + c);
-    float2 q = old;
+  auto pnew = [&](long long c, F4& q, F4& old) {
+    old.load(pold, c);
+    q = old;
     if (upd) {
-      const float2 s = *reinterpret_cast<const float2*>(r + c);
-      q.x = fmaf(beta, q.x, s.x);
-      q.y = fmaf(beta, q.y, s.y);
+      F4 s;
+      s.load(r, c);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) q.v[i] = fmaf(beta, old.v[i], s.v[i]);
     }
-    return q;
   };
   auto pnew1 = [&](long long c) { return upd ? fmaf(beta, pold[c], r[c]) : pold[c]; };
   Dot2 dot;
-  float2 pm = make_float2(0.f, 0.f), pc = pm, pnx = pm, cyc = pm, oc = pm, onx = pm, junk;
+  F4 pm{}, pc{}, pnx{}, cyc{}, oc{}, onx{}, junk{};
   if (active) {
-    pc = pnew(L.at(ja, k0), oc);
-    pm = (k0 == 1) ? pc : pnew(L.at(ja, k0 - 1), junk);
-    cyc = *reinterpret_cast<const float2*>(m.cy + L.at(ja, k0));
+    pnew(L.at(ja, k0), pc, oc);
+    if (k0 == 1)
+      pm = pc;
+    else
+      pnew(L.at(ja, k0 - 1), pm, junk);
+    cyc.load(m.cy, L.at(ja, k0));
   }
   for (int k = k0; k <= k1; ++k) {
     const int b = k & 1;
     if (active) {
-      pnx = (k == L.ny) ? pc : pnew(L.at(ja, k + 1), onx);
-      buf[b][2 * t + 1] = pc.x;
-      buf[b][2 * t + 2] = pc.y;
+      if (k == L.ny)
+        pnx = pc;
+      else
+        pnew(L.at(ja, k + 1), pnx, onx);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) buf[b][4 * t + 1 + i] = pc.v[i];
     }
     if (t == 0 && js > 1) buf[b][0] = pnew1(L.at(js - 1, k));
     if (t == MT - 1 && js + MSW <= L.nx) buf[b][MSW + 1] = pnew1(L.at(js + MSW, k));
     __syncthreads();
     if (active) {
       const long long c = L.at(ja, k);
-      const float2 cyn = *reinterpret_cast<const float2*>(m.cy + c + L.ld);
-      const float2 cxa = *reinterpret_cast<const float2*>(m.cx + c);
-      const float2 dd = *reinterpret_cast<const float2*>(m.di + c);
-      const float left_a = (ja == 1) ? pc.x : buf[b][ja - js];
-      const float right_a = has_b ? pc.y : pc.x;
-      float wa = dd.x * pc.x;
-      wa = fmaf(-cyn.x, pnx.x, wa);
-      wa = fmaf(-cyc.x, pm.x, wa);
-      wa = fmaf(-cxa.y, right_a, wa);
-      wa = fmaf(-cxa.x, left_a, wa);
-      dot.add(wa, pc.x);
-      if (has_b) {
-        const float cxr = m.cx[c + 2];
-        const float right_b = (ja + 1 == L.nx) ? pc.y : buf[b][ja - js + 3];
-        float wb = dd.y * pc.y;
-        wb = fmaf(-cyn.y, pnx.y, wb);
-        wb = fmaf(-cyc.y, pm.y, wb);
-        wb = fmaf(-cxr, right_b, wb);
-        wb = fmaf(-cxa.y, pc.x, wb);
-        dot.add(wb, pc.y);
-        *reinterpret_cast<float2*>(m.w + c) = make_float2(wa, wb);
-        *reinterpret_cast<float2*>(pout + c) = pc;
-        if (upd_d) {
-          float2 dv = *reinterpret_cast<const float2*>(m.d + c);
-          dv.x = fmaf(da, oc.x, dv.x);
-          dv.y = fmaf(da, oc.y, dv.y);
-          *reinterpret_cast<float2*>(m.d + c) = dv;
-        }
-      } else {
-        m.w[c] = wa;
-        pout[c] = pc.x;
-        if (upd_d) m.d[c] = fmaf(da, oc.x, m.d[c]);
+      F4 cyn, cx4, dd, w;
+      cyn.load(m.cy, c + L.ld);
+      cx4.load(m.cx, c);
+      dd.load(m.di, c);
+      const float cxr = (nv == 4) ? m.cx[c + 4] : 0.f;
+      const float left0 = (ja == 1) ? pc.v[0] : buf[b][4 * t];
+      const float right3 = buf[b][4 * t + 5];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const float left = (i == 0) ? left0 : pc.v[i - 1];
+        float right = (i < 3) ? pc.v[i + 1] : right3;
+        if (ja + i == L.nx) right = pc.v[i];  // mirror at the domain edge
+        const float cright = (i < 3) ? cx4.v[i + 1] : cxr;
+        float a = dd.v[i] * pc.v[i];
+        a = fmaf(-cyn.v[i], pnx.v[i], a);
+        a = fmaf(-cyc.v[i], pm.v[i], a);
+        a = fmaf(-cright, right, a);
+        a = fmaf(-cx4.v[i], left, a);
+        w.v[i] = a;
+        if (i < nv) dot.add(a, pc.v[i]);
+      }
+      w.store(m.w, c, nv);
+      pc.store(pout, c, nv);
+      if (upd_d) {
+        F4 dv;
+        dv.load(m.d, c);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) dv.v[i] = fmaf(da, oc.v[i], dv.v[i]);
+        dv.store(m.d, c, nv);
       }
       cyc = cyn;
     }
@@ -221,47 +253,56 @@ __global__ void __launch_bounds__(MT) k_mix_w(MixFields m, Layout L, Reduce rd, 
   grid_reduce<1>(acc, rd, EpiMixW{ms});
 }
 
-// r -= alpha w (FP32), r.r (Dot2), inner epilogue.
+// r -= alpha w (FP32), r.r (Dot2), inner epilogue.  Four columns per thread.
 __global__ void __launch_bounds__(MT) k_mix_ur(MixFields m, Layout L, Reduce rd, MixState* ms) {
   if (ms->status != RUN) return;
   const float alpha = (float)ms->alpha;
-  const int ja = blockIdx.x * MSW + 1 + 2 * threadIdx.x;
-  const bool has_b = ja + 1 <= L.nx;
+  const int ja = blockIdx.x * MSW + 1 + 4 * threadIdx.x;
+  const int nv = min(4, L.nx - ja + 1);
   Dot2 dot;
-  if (ja <= L.nx) {
+  if (nv > 0) {
     for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
       const long long c = L.at(ja, k);
-      const float2 ww = *reinterpret_cast<const float2*>(m.w + c);
-      float2 rr = *reinterpret_cast<const float2*>(m.r + c);
-      rr.x = fmaf(-alpha, ww.x, rr.x);
-      rr.y = fmaf(-alpha, ww.y, rr.y);
-      dot.add(rr.x, rr.x);
-      if (has_b) {
-        dot.add(rr.y, rr.y);
-        *reinterpret_cast<float2*>(m.r + c) = rr;
-      } else {
-        m.r[c] = rr.x;
+      F4 ww, rr;
+      ww.load(m.w, c);
+      rr.load(m.r, c);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        rr.v[i] = fmaf(-alpha, ww.v[i], rr.v[i]);
+        if (i < nv) dot.add(rr.v[i], rr.v[i]);
       }
+      rr.store(m.r, c, nv);
     }
   }
   double acc[1] = {dot.value()};
   grid_reduce<1>(acc, rd, EpiMixUr{ms});
 }
 
-// pending d += alpha p, then u += d in FP64 (one pass per outer iteration)
-__global__ void k_mix_apply(Fields f, MixFields m, Layout L, MixState* ms) {
+
+// d += alpha p when the deferred update of the last step is pending.
+__global__ void k_mix_flush_d(MixFields m, Layout L, MixState* ms) {
+  if (!ms->d_pending) return;
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (j > L.nx) return;
-  const bool pend = ms->d_pending != 0;
   const float da = (float)ms->d_alpha;
   const float* __restrict__ p = ms->d_psel ? m.p2 : m.p;
   for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
     const long long c = L.at(j, k);
-    float d = m.d[c];
-    if (pend) d = fmaf(da, p[c], d);
-    f.u[c] = f.u[c] + (double)d;
+    m.d[c] = fmaf(da, p[c], m.d[c]);
   }
 }
+
+// Accept the correction: u += d in FP64, d = 0.
+__global__ void k_mix_apply(Fields f, MixFields m, Layout L) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (j > L.nx) return;
+  for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
+    const long long c = L.at(j, k);
+    f.u[c] = f.u[c] + (double)m.d[c];
+    m.d[c] = 0.f;
+  }
+}
+
 
 inline int mstrips(const Layout& L) { return (L.nx + MSW - 1) / MSW; }
 
@@ -272,10 +313,15 @@ void launch_mix_prep(const Fields& f, const MixFields& m, const Layout& L, cudaS
   { ++launch_counter(); k_mix_prep<<<grid, 256, 0, s>>>(f, m, L); }
 }
 
-void launch_mix_residual(const Fields& f, const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms,
-                         cudaStream_t s) {
+void launch_mix_trial(const Fields& f, const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms,
+                      bool first, cudaStream_t s) {
   dim3 grid((L.nx + 255) / 256, L.ny < 256 ? L.ny : 256);
-  { ++launch_counter(); k_mix_residual<<<grid, 256, 0, s>>>(f, m, L, rd, ms); }
+  { ++launch_counter(); k_mix_trial<<<grid, 256, 0, s>>>(f, m, L, rd, ms, first); }
+}
+
+void launch_mix_flush_d(const MixFields& m, const Layout& L, MixState* ms, cudaStream_t s) {
+  dim3 grid((L.nx + 255) / 256, L.ny < 4096 ? L.ny : 4096);
+  { ++launch_counter(); k_mix_flush_d<<<grid, 256, 0, s>>>(m, L, ms); }
 }
 
 void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms, cudaStream_t s) {
@@ -290,9 +336,9 @@ void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd,
   { ++launch_counter(); k_mix_ur<<<dim3(ns, gy), MT, 0, s>>>(m, L, rd, ms); }
 }
 
-void launch_mix_apply(const Fields& f, const MixFields& m, const Layout& L, MixState* ms, cudaStream_t s) {
+void launch_mix_apply(const Fields& f, const MixFields& m, const Layout& L, cudaStream_t s) {
   dim3 grid((L.nx + 255) / 256, L.ny < 4096 ? L.ny : 4096);
-  { ++launch_counter(); k_mix_apply<<<grid, 256, 0, s>>>(f, m, L, ms); }
+  { ++launch_counter(); k_mix_apply<<<grid, 256, 0, s>>>(f, m, L); }
 }
 
 }  // namespace tl

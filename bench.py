@@ -15,7 +15,8 @@ value  : device time (CUDA events on the solver stream) of the K timed steps, in
 e2e    : the same steps through the C ABI with host buffers: density/energy uploaded from
          pinned host memory, solve, energy downloaded, every step (host wall clock).
 roofline: the dominant kernel (fused p-update + matvec + p.w sweep) timed per launch with
-         CUDA events during the timed steps, against 48 B/cell of compulsory traffic.
+         CUDA events during the timed steps, against 64 B/cell of compulsory traffic (the
+         p update and matvec streams plus the deferred u += alpha p of the previous step).
 cpu_baseline: the CPU port (oracle/, OpenMP over all host cores) on a bounded sample of
          the same workload (one time-step solve capped at --cpu-iters iterations).
 
@@ -37,7 +38,10 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-BYTES_PER_CELL_MATVEC = 48  # r, p_old, Kx, Ky read; p, w written (8 B each)
+# compulsory traffic of the fused sweep: r, p_old, Kx, Ky, u read; p, w, u written (8 B each).
+# The u += alpha p of the previous step is folded into it; Di (stored, 8 B more) is not
+# counted because the reference recomputes it from Kx, Ky.
+BYTES_PER_CELL_MATVEC = 64
 BYTES_PER_CELL_IT = 96      # whole FP64 CG iteration (12 streams)
 FALLBACK_HBM_GBS = 6800.0
 
@@ -54,6 +58,11 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="form timed in the main loop (mixed: FP32 CG steps with FP64 residual replacement)")
+    ap.add_argument("--no-mixed-compare", action="store_true",
+                    help="skip the full-solve FP64 vs mixed time-to-solution comparison")
+    ap.add_argument("--delta", type=float, default=0.0, help="mixed: residual replacement factor (0: library default)")
     return ap.parse_args()
 
 
@@ -192,6 +201,48 @@ def cpu_port_steps(d, iters, steps, warmup, density=None, energy=None):
     return sum(times), its, cores
 
 
+def mixed_vs_fp64(chunk, d, args):
+    """Time to solution of the first time step of the workload (generated initial state,
+    tl_eps 1e-15, no iteration cap) in the FP64 form and in the mixed form.  Both results'
+    true residuals ||u0 - A u|| are computed in FP64 after the solve (tl_calc_residual,
+    tl_calc_2norm), and the mixed result's field summary and u are compared with the FP64
+    form's.  The chunk's state is restored afterwards."""
+    import numpy as np
+
+    from tealeaf_ref_gb300 import native
+
+    dens0 = chunk.download("density")
+    ener0 = chunk.download("energy1")
+    chunk.generate(d)
+    dens = chunk.download("density")
+    ener = chunk.download("energy1")
+    full = d.replace(max_iters=200000)
+    out = {}
+    runs = {}
+    for prec in ("fp64", "mixed"):
+        chunk.upload_state(dens, ener)
+        info = chunk.tea_leaf(native.opts_from_deck(full, prec, inner_tol=args.delta), full.initial_timestep)
+        summary, u = chunk.field_summary(), chunk.download("u")
+        chunk.update_halo(["u"])
+        chunk.calc_residual()
+        true_res = float(np.sqrt(abs(chunk.calc_2norm(1))))
+        runs[prec] = (info, summary, u)
+        out[prec] = {"seconds": info.solve_seconds, "iterations": info.reported_iterations,
+                     "relative_true_residual": true_res / info.initial_residual}
+        if prec == "mixed":
+            out[prec].update(residual_replacements=info.outer_iterations,
+                             stop=native.STOP_REASONS.get(info.stop_reason, "?"),
+                             true_residual_over_floor=info.true_residual / info.residual_floor)
+    (i64, s64, u64), (imx, smx, umx) = runs["fp64"], runs["mixed"]
+    out["time_ratio_mixed_over_fp64"] = imx.solve_seconds / i64.solve_seconds
+    out["field_summary_max_rel_diff"] = float(np.max(np.abs(smx - s64) / np.abs(s64)))
+    out["u_max_rel_diff"] = float(np.max(np.abs(umx - u64) / np.abs(u64)))
+    out["workload"] = "first time step of the %dx%d workload from its generated state, tl_eps %g" % (
+        args.cells, args.cells, full.eps)
+    chunk.upload_state(dens0, ener0)
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -248,7 +299,7 @@ def main():
 
     native.set_device(local)
     d = workload(args)
-    opts = native.opts_from_deck(d)
+    opts = native.opts_from_deck(d, args.precision, inner_tol=args.delta)
     dt = d.initial_timestep
     cells = args.cells * args.cells
 
@@ -349,6 +400,10 @@ def main():
         "note": "FP64 issue rate (measured 0.60 T DFMA/s) bounds the sweep before HBM does",
     }
 
+    mixed_cmp = None
+    if rank == 0 and world == 1 and not args.no_mixed_compare:
+        mixed_cmp = mixed_vs_fp64(chunk, d, args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -364,7 +419,8 @@ def main():
 
     if rank == 0:
         out = {
-            "metric": "CG cell-iterations/s (FP64, %d^2)" % args.cells,
+            "metric": ("CG cell-iterations/s (FP64, %d^2)" % args.cells if args.precision == "fp64" else
+                       "CG cell-iterations/s (FP32 steps with FP64 residual replacement, %d^2)" % args.cells),
             "value": value,
             "unit": "cell-iterations/s",
             "n_gpus": world,
@@ -374,11 +430,13 @@ def main():
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64",
+            "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic",
-            "config": dict(config_json(args, d), parallelism="replicas" if world > 1 else "single"),
+            "config": dict(config_json(args, d), parallelism="replicas" if world > 1 else "single",
+                           precision=args.precision),
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "mixed_vs_fp64": mixed_cmp,
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk.summary(),

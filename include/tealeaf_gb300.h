@@ -89,7 +89,7 @@ typedef struct tl_solve_opts {
    * u0 - A u (the CG search direction is kept across replacements). */
   int precision;
   double inner_tol;      /* mixed: replace the residual each time it has fallen by this
-                            factor since the last replacement (0: 0.1) */
+                            factor since the last replacement (0: 0.5) */
   int max_inner_iters;   /* mixed: cap on FP32 CG steps (0: max_iters) */
 } tl_solve_opts;
 
@@ -110,10 +110,20 @@ typedef struct tl_solve_info {
   double eigmin, eigmax;
   double solve_seconds;     /* device time of the whole call (CUDA events on its stream) */
   long long kernel_launches; /* kernels this call launched */
-  int outer_iterations;     /* mixed: refinement steps (0 for the FP64 form) */
-  int pad_;
+  int outer_iterations;     /* mixed: accepted residual replacements (0 for the FP64 form) */
+  int stop_reason;          /* mixed: TL_STOP_* (0 for the FP64 form) */
   double true_residual;     /* mixed: final sqrt(|u0 - A u|^2) computed in FP64 */
+  double residual_floor;    /* mixed: eps_64 * ||(|u0| + |Di u| + sum |c u_nb|)||_2 of the
+                               final u, the rounding level of the FP64 residual */
 } tl_solve_info;
+
+/* Why the mixed-precision solve stopped (tl_solve_info.stop_reason). */
+#define TL_STOP_EPS 1      /* true residual < tl_eps * initial residual (tea_solve.f90:410) */
+#define TL_STOP_FLOOR 2    /* true residual within TL_FLOOR_FACTOR of residual_floor */
+#define TL_STOP_STALL 3    /* three replacements in a row each lowered it by < 10% */
+#define TL_STOP_REJECT 4   /* two corrections in a row did not lower it */
+#define TL_STOP_CAP 5      /* max_inner_iters FP32 CG steps */
+#define TL_FLOOR_FACTOR 16.0
 
 /* Kernel ids for the per-kernel timers (tl_profile_read). */
 #define TL_KERNEL_CG_MATVEC 0 /* fused p update + w = A p + p.w sweep of the CG loop */

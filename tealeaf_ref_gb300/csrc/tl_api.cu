@@ -1,6 +1,7 @@
 // tl_api.cu -- the C ABI (include/tealeaf_gb300.h): context, host<->device copies, the
 // per-kernel drop-in entry points and tl_tea_leaf(), a C++ restatement of the control flow
 // of tea_leaf() (tea_solve.f90:37-503) over the GPU kernels.
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -721,6 +722,20 @@ int sync_mix(tl_ctx* c) {
   return TL_OK;
 }
 
+// Starts a fresh FP32 CG process on the correction (d must be zero): r = p = u0 - A u.
+int mix_restart(tl_ctx* c, const Reduce& rd, double* floor_est) {
+  MixState& H = *c->mst_host;
+  launch_mix_trial(c->f, c->mix, c->L, rd, c->mst, true, c->stream);
+  int rc;
+  if ((rc = check_launch("mixed restart"))) return rc;
+  if ((rc = sync_mix(c))) return rc;
+  *floor_est = DBL_EPSILON * std::sqrt(H.trial_scale);
+  H.rro = H.rr = H.rr_max = H.trial_rr32;
+  H.p_pending = 0;
+  H.status = RUN;
+  return TL_OK;
+}
+
 // Mixed-precision CG (tl_mixed.cu): FP64 refinement loop around FP32 inner CG solves.
 // Called by tl_tea_leaf after the set-up kernels; finishes the solve (finalise included).
 int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long launches0) {
@@ -728,10 +743,11 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
   if ((rc = ensure_mix(c))) return rc;
   MixState& H = *c->mst_host;
   memset(&H, 0, sizeof(H));
-  const double delta = o->inner_tol > 0.0 ? o->inner_tol : 0.1;
+  const double delta = o->inner_tol > 0.0 ? o->inner_tol : 0.5;
   H.delta2 = delta * delta;
   H.max_n = o->max_inner_iters > 0 ? std::min(o->max_inner_iters, o->max_iters) : o->max_iters;
   H.phase_end = 0x7fffffff;
+  H.n = 1;  // step counter; the set-up trial puts p in the buffer step 1 reads
   const Reduce rd = c->rd();
   const size_t fbytes = (size_t)c->L.elems() * sizeof(float);
   CK(cudaMemsetAsync(c->mix.d, 0, fbytes, c->stream));  // a rejected correction may remain
@@ -747,22 +763,29 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
   H.d_pending = 0;
   H.status = (H.trial_rr32 > 0.0 && std::isfinite(H.trial_rr32)) ? RUN : EXIT_CONVERGED;
   double res = initial_residual, prev = initial_residual;
-  int outer = 0, last_phase = 0;
+  double floor_est = DBL_EPSILON * std::sqrt(H.trial_scale);
+  int outer = 0, stalled = 0, stop = TL_STOP_EPS;
+  bool rejected = false, stall_restarted = false;
   const int batch = tl_ctx::BATCH;
-  while (res >= o->eps * initial_residual && H.status == RUN) {
+  while (H.status == RUN) {
+    if (res < o->eps * initial_residual) {  // the reference's convergence test
+      stop = TL_STOP_EPS;
+      break;
+    }
+    if (res <= TL_FLOOR_FACTOR * floor_est) {  // no correction can lower it much further
+      stop = TL_STOP_FLOOR;
+      break;
+    }
     // FP32 CG steps until the recursive residual has fallen by delta since the last
-    // replacement; after the first phase each phase gets a step budget, so a process that
-    // has lost its way near the accuracy floor is stopped and checked
-    H.phase_end = last_phase > 0 ? H.n + std::max(64, 4 * last_phase) : 0x7fffffff;
+    // replacement (or the overall step cap)
+    H.phase_end = 0x7fffffff;
     CK(cudaMemcpyAsync(c->mst, &H, sizeof(MixState), cudaMemcpyHostToDevice, c->stream));
-    const int n_start = H.n;
     while (H.status == RUN) {
       for (int i = 0; i < batch; ++i) launch_mix_iteration(c->mix, c->L, rd, c->mst, c->stream);
       if ((rc = check_launch("mixed batch"))) return rc;
       if ((rc = sync_mix(c))) return rc;
     }
     if (H.status == EXIT_BREAKDOWN) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite FP32 CG scalar");
-    last_phase = H.n - n_start;
     const bool capped = H.n > H.max_n;
     // trial replacement: true FP64 residual of u + d, u itself untouched
     launch_mix_flush_d(c->mix, c->L, c->mst, c->stream);  // the trial's epilogue clears d_pending
@@ -771,19 +794,49 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
     if ((rc = sync_mix(c))) return rc;
     const double res_t = std::sqrt(std::fabs(H.trial_rr));
     if (!std::isfinite(res_t)) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite residual");
-    if (!(res_t < prev)) break;  // no gain: keep u, drop the correction
+    if (!(res_t < prev)) {
+      // no gain: keep u and drop the correction.  Restart the FP32 process from the true
+      // residual of u with a fresh direction; a second failure in a row means u sits at the
+      // FP64 accuracy floor of u0 - A u.
+      if (rejected || capped) {
+        stop = capped ? TL_STOP_CAP : TL_STOP_REJECT;
+        break;
+      }
+      rejected = true;
+      CK(cudaMemsetAsync(c->mix.d, 0, fbytes, c->stream));
+      if ((rc = mix_restart(c, rd, &floor_est))) return rc;
+      continue;
+    }
     launch_mix_apply(c->f, c->mix, c->L, c->stream);  // accept: u += d, d = 0
     ++outer;
-    res = res_t;
-    // at the FP64 accuracy floor of u0 - A u the true residual stops falling
-    if (capped || res > 0.5 * prev) break;
-    prev = res;
+    rejected = false;
+    floor_est = DBL_EPSILON * std::sqrt(H.trial_scale);
+    // replacements that keep gaining less than 10% each: restart the FP32 process once with a
+    // fresh direction; if that does not bring back a 10% gain, u has reached the floor
+    stalled = (res_t > 0.9 * prev) ? stalled + 1 : 0;
+    if (stalled == 0) stall_restarted = false;
+    res = prev = res_t;
+    if (capped) {
+      stop = TL_STOP_CAP;
+      break;
+    }
+    if (stalled >= 3) {
+      if (stall_restarted) {
+        stop = TL_STOP_STALL;
+        break;
+      }
+      stall_restarted = true;
+      stalled = 0;
+      if ((rc = mix_restart(c, rd, &floor_est))) return rc;  // d was zeroed by the apply
+      continue;
+    }
     // continue the CG process with r replaced by the true residual, search direction kept
     H.beta = H.trial_rr32 / H.rro_prev;
     H.rro = H.rr = H.rr_max = H.trial_rr32;
     H.p_pending = 1;
     H.status = RUN;
   }
+  if (res < o->eps * initial_residual) stop = TL_STOP_EPS;
   const int inner_total = H.n - 1;
   launch_finalise(c->f, c->L, c->stream);
   if ((rc = do_halo(c, M(TL_FIELD_ENERGY1), 1))) return rc;
@@ -799,6 +852,8 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
   info->error = res;
   info->exact_error = res;
   info->true_residual = res;
+  info->residual_floor = floor_est;
+  info->stop_reason = stop;
   info->outer_iterations = outer;
   info->solve_seconds = ms * 1e-3;
   info->kernel_launches = launch_counter() - launches0;

@@ -92,6 +92,7 @@ struct MixState {
   double delta2;                              // replace when r.r < delta2 * rr_max
   double trial_rr;                            // ||u0 - A (u + d)||^2 in FP64 (last trial)
   double trial_rr32;                          // r.r of its FP32 rounding
+  double trial_scale;                         // sum of (|u0| + |Di u| + sum |c u_nb|)^2 (last trial)
   double d_alpha;
   int n, max_n, phase_end, status, p_pending, d_pending, d_psel;
 };

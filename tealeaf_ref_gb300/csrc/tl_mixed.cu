@@ -60,9 +60,10 @@ __device__ __forceinline__ void mix_finish(MixState* ms) {
 // The pending d update was flushed before the trial (k_mix_flush_d), so it is cleared here.
 struct EpiMixTrial {
   MixState* ms;
-  __device__ void operator()(double (&acc)[2]) const {
+  __device__ void operator()(double (&acc)[3]) const {
     ms->trial_rr = acc[0];
     ms->trial_rr32 = acc[1];
+    ms->trial_scale = acc[2];
     ms->d_pending = 0;
   }
 };
@@ -112,10 +113,15 @@ __global__ void k_mix_prep(Fields f, MixFields m, Layout L) {
 
 // Trial residual in FP64 of the corrected solution: r = u0 - A (u + d), with off-domain
 // neighbours mirrored (the reflective halo copy, or a value multiplied by a zero boundary
-// coefficient), so u's halo is not needed.  r32 = r; ||r||^2 and ||r32||^2 in FP64.
-// first: the start of the CG process, p32 = r32.
+// coefficient), so u's halo is not needed.  r32 = r; ||r||^2 and ||r32||^2 in FP64, and the
+// squared norm of the per-cell magnitude sum |u0| + |Di u| + sum |c u_nb|: FP64 rounding of u
+// and of the residual arithmetic leaves r uncertain by a small multiple of eps_64 times it,
+// the level below which no correction can lower the true residual.
+// first: the start of the CG process, p32 = r32 in the buffer the next k_mix_w reads as its
+// previous direction.
 __global__ void k_mix_trial(Fields f, MixFields m, Layout L, Reduce rd, MixState* ms, bool first) {
-  double acc[2] = {0.0, 0.0};
+  double acc[3] = {0.0, 0.0, 0.0};
+  float* __restrict__ p0 = (ms->n & 1) ? m.p : m.p2;
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
     if (j > L.nx) continue;
@@ -134,10 +140,13 @@ __global__ void k_mix_trial(Fields f, MixFields m, Layout L, Reduce rd, MixState
     acc[0] = fma(r, r, acc[0]);
     const float r32 = (float)r;
     m.r[c] = r32;
-    if (first) m.p[c] = r32;
+    if (first) p0[c] = r32;
     acc[1] = fma((double)r32, (double)r32, acc[1]);
+    const double s = fabs(f.u0[c]) + fabs(f.di[c] * uc) + fabs(f.cy[c + L.ld] * ut) + fabs(f.cy[c] * ub) +
+                     fabs(f.cx[c + 1] * ur) + fabs(f.cx[c] * ul);
+    acc[2] = fma(s, s, acc[2]);
   }
-  grid_reduce<2>(acc, rd, EpiMixTrial{ms});
+  grid_reduce<3>(acc, rd, EpiMixTrial{ms});
 }
 
 
@@ -200,6 +209,9 @@ __global__ void __launch_bounds__(MT) k_mix_w(MixFields m, Layout L, Reduce rd, 
   }
   for (int k = k0; k <= k1; ++k) {
     const int b = k & 1;
+    const long long c = L.at(ja, k);
+    F4 cyn, cx4, dd, dv, w;
+    float cxr = 0.f;
     if (active) {
       if (k == L.ny)
         pnx = pc;
@@ -207,17 +219,18 @@ __global__ void __launch_bounds__(MT) k_mix_w(MixFields m, Layout L, Reduce rd, 
         pnew(L.at(ja, k + 1), pnx, onx);
 #pragma unroll
       for (int i = 0; i < 4; ++i) buf[b][4 * t + 1 + i] = pc.v[i];
+      // this row's coefficient (and correction) loads are issued before the barrier so
+      // that their latency overlaps the wait
+      cyn.load(m.cy, c + L.ld);
+      cx4.load(m.cx, c);
+      dd.load(m.di, c);
+      if (nv == 4) cxr = m.cx[c + 4];
+      if (upd_d) dv.load(m.d, c);
     }
     if (t == 0 && js > 1) buf[b][0] = pnew1(L.at(js - 1, k));
     if (t == MT - 1 && js + MSW <= L.nx) buf[b][MSW + 1] = pnew1(L.at(js + MSW, k));
     __syncthreads();
     if (active) {
-      const long long c = L.at(ja, k);
-      F4 cyn, cx4, dd, w;
-      cyn.load(m.cy, c + L.ld);
-      cx4.load(m.cx, c);
-      dd.load(m.di, c);
-      const float cxr = (nv == 4) ? m.cx[c + 4] : 0.f;
       const float left0 = (ja == 1) ? pc.v[0] : buf[b][4 * t];
       const float right3 = buf[b][4 * t + 5];
 #pragma unroll
@@ -237,8 +250,6 @@ __global__ void __launch_bounds__(MT) k_mix_w(MixFields m, Layout L, Reduce rd, 
       w.store(m.w, c, nv);
       pc.store(pout, c, nv);
       if (upd_d) {
-        F4 dv;
-        dv.load(m.d, c);
 #pragma unroll
         for (int i = 0; i < 4; ++i) dv.v[i] = fmaf(da, oc.v[i], dv.v[i]);
         dv.store(m.d, c, nv);
@@ -261,17 +272,29 @@ __global__ void __launch_bounds__(MT) k_mix_ur(MixFields m, Layout L, Reduce rd,
   const int nv = min(4, L.nx - ja + 1);
   Dot2 dot;
   if (nv > 0) {
-    for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
-      const long long c = L.at(ja, k);
-      F4 ww, rr;
-      ww.load(m.w, c);
-      rr.load(m.r, c);
+    // four rows per pass with every load issued before any use (memory-level parallelism)
+    const int gy = gridDim.y;
+    for (int k = blockIdx.y + 1; k <= L.ny; k += 4 * gy) {
+      F4 ww[4], rr[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        rr.v[i] = fmaf(-alpha, ww.v[i], rr.v[i]);
-        if (i < nv) dot.add(rr.v[i], rr.v[i]);
+      for (int u = 0; u < 4; ++u) {
+        if (k + u * gy <= L.ny) {
+          const long long c = L.at(ja, k + u * gy);
+          ww[u].load(m.w, c);
+          rr[u].load(m.r, c);
+        }
       }
-      rr.store(m.r, c, nv);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (k + u * gy <= L.ny) {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            rr[u].v[i] = fmaf(-alpha, ww[u].v[i], rr[u].v[i]);
+            if (i < nv) dot.add(rr[u].v[i], rr[u].v[i]);
+          }
+          rr[u].store(m.r, L.at(ja, k + u * gy), nv);
+        }
+      }
     }
   }
   double acc[1] = {dot.value()};

@@ -35,6 +35,8 @@ class TeaLeafError(RuntimeError):
 
 
 PRECISION = {"fp64": 0, "mixed": 1}
+# tl_solve_info.stop_reason of the mixed form (TL_STOP_*)
+STOP_REASONS = {0: "none", 1: "eps", 2: "floor", 3: "stall", 4: "reject", 5: "cap"}
 
 
 class SolveOpts(C.Structure):
@@ -48,8 +50,8 @@ class SolveInfo(C.Structure):
                 ("cg_calc_steps", C.c_int), ("cheby_calc_steps", C.c_int), ("est_itc", C.c_int),
                 ("initial_residual", C.c_double), ("error", C.c_double), ("exact_error", C.c_double),
                 ("eigmin", C.c_double), ("eigmax", C.c_double), ("solve_seconds", C.c_double),
-                ("kernel_launches", C.c_longlong), ("outer_iterations", C.c_int), ("pad_", C.c_int),
-                ("true_residual", C.c_double)]
+                ("kernel_launches", C.c_longlong), ("outer_iterations", C.c_int), ("stop_reason", C.c_int),
+                ("true_residual", C.c_double), ("residual_floor", C.c_double)]
 
     def as_dict(self):
         return {f[0]: getattr(self, f[0]) for f in self._fields_}

@@ -33,7 +33,13 @@ def test_mixed_cg_matches_fp64_oracle(case):
     ro = oracle.run_deck(d)
     opts = native.opts_from_deck(d, precision="mixed")
     with native.Chunk.from_deck(d) as c:
-        infos = [c.tea_leaf(opts, d.initial_timestep) for _ in range(d.end_step)]
+        infos, recomputed = [], []
+        for _ in range(d.end_step):
+            infos.append(c.tea_leaf(opts, d.initial_timestep))
+            # the true residual the solve reports, recomputed by the per-kernel entry points
+            c.update_halo(["u"])
+            c.calc_residual()
+            recomputed.append(np.sqrt(abs(c.calc_2norm(1))))
         s = c.field_summary()
         u = c.download("u")
     o = oracle.Chunk.from_deck(d)
@@ -41,9 +47,26 @@ def test_mixed_cg_matches_fp64_oracle(case):
         o.tea_leaf(d)
     assert _rel(s, ro.summaries[-1][1]) < 1e-10
     assert _rel(u, np.array(o.interior("u"))) < 1e-8
-    for i in infos:
+    for i, rr in zip(infos, recomputed):
         assert i.outer_iterations >= 1
         assert i.true_residual <= 1e-9 * i.initial_residual
+        assert native.STOP_REASONS[i.stop_reason] in ("eps", "floor", "stall", "reject")
+        assert 0.0 < i.residual_floor < i.true_residual * 1e3
+        # near the floor the residual is rounding noise, so the two evaluations agree in size only
+        assert rr <= 2.0 * i.true_residual + 16.0 * i.residual_floor
+
+
+def test_mixed_cg_inner_cap():
+    """max_inner_iters stops the FP32 CG process; the accepted corrections remain in u."""
+    from tealeaf_ref_gb300 import native
+
+    d = small_deck(nx=64, ny=64, steps=1, n_rect=3, n_circ=1, max_iters=20000)
+    opts = native.opts_from_deck(d, precision="mixed", max_inner_iters=12)
+    with native.Chunk.from_deck(d) as c:
+        i = c.tea_leaf(opts, d.initial_timestep)
+    assert native.STOP_REASONS[i.stop_reason] == "cap"
+    assert i.reported_iterations == 12
+    assert i.true_residual < i.initial_residual
 
 
 def test_mixed_cg_reference_deck(golden):

@@ -63,6 +63,10 @@ def parse():
     ap.add_argument("--no-mixed-compare", action="store_true",
                     help="skip the full-solve FP64 vs mixed time-to-solution comparison")
     ap.add_argument("--delta", type=float, default=0.0, help="mixed: residual replacement factor (0: library default)")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="instead of the CG line: the adjoint problem (2048^2, 10 steps; gradient of "
+                         "sum (u - u_target)^2 wrt density), forward + reverse time and finite-difference checks")
+    ap.add_argument("--fd-cells", type=int, default=8, help="adjoint: cells for the per-cell difference check")
     return ap.parse_args()
 
 
@@ -243,6 +247,79 @@ def mixed_vs_fp64(chunk, d, args):
     return out
 
 
+def run_adjoint(args):
+    """The adjoint problem: density and energy from the seeded generator (8 rectangles, seed 4),
+    u_target from a forward run on density * (1 + 0.01 N(0,1)) (seed 4), loss
+    sum (u_final - u_target)^2 after 10 FP64 CG time steps, gradient wrt the per-cell density by
+    the reverse sweep (tl_adjoint_*), with each step's u checkpointed on the device.  Checked
+    by central differences of the same forward: along a seeded +-1 direction scaled by density
+    (h 1e-5), and per cell (4th-order, h 1e-3 relative) on seeded cells among those whose
+    gradient is at least 0.1 of the largest -- cells with smaller gradients change L by less
+    than the rounding noise of the forward solves (~1e-11 of L)."""
+    import numpy as np
+
+    from tealeaf_ref_gb300 import deck as dk
+    from tealeaf_ref_gb300 import native
+    from tealeaf_ref_gb300.adjoint import forward_loss, perturbed_density, squared_error_gradient
+
+    cells = args.cells if args.cells != 8192 else 2048
+    d = dk.config_deck(4, cells=cells)
+    T, dt = d.end_step, d.initial_timestep
+    opts = native.opts_from_deck(d)
+    with native.Chunk.from_deck(d) as c:
+        rho, e0 = c.download("density"), c.download("energy1")
+        forward_loss(c, perturbed_density(rho, 4), e0, np.zeros_like(rho), opts, dt, T)
+        target = c.download("u")
+        t0 = time.perf_counter()
+        loss0 = forward_loss(c, rho, e0, target, opts, dt, T)
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        loss, g, _, rinfo = squared_error_gradient(c, rho, e0, target, opts, dt, T, rho_only=True)
+        t_both = time.perf_counter() - t0
+        rng = np.random.Generator(np.random.PCG64(4))
+        v = rho * rng.choice([-1.0, 1.0], size=rho.shape)
+        h = 1e-5
+        fd_dir = (forward_loss(c, rho + h * v, e0, target, opts, dt, T) -
+                  forward_loss(c, rho - h * v, e0, target, opts, dt, T)) / (2 * h)
+        g_dir = float(np.sum(g * v))
+        gmax = float(np.max(np.abs(g)))
+        big = np.argwhere(np.abs(g) >= 0.1 * gmax)
+        pick = big[rng.choice(len(big), size=min(args.fd_cells, len(big)), replace=False)]
+        per_cell = []
+        for idx in map(tuple, pick):
+            hh = 1e-3 * rho[idx]
+
+            def at(s):
+                p = rho.copy()
+                p[idx] += s * hh
+                return forward_loss(c, p, e0, target, opts, dt, T)
+
+            fd = (8 * (at(1) - at(-1)) - (at(2) - at(-2))) / (12 * hh)
+            per_cell.append({"cell": [int(idx[0]), int(idx[1])], "grad": float(g[idx]), "fd": fd,
+                             "rel_err": abs(fd - g[idx]) / abs(g[idx])})
+    out = {
+        "metric": "adjoint: forward + reverse time for d/d(density) of sum (u - u_target)^2 (FP64, %d^2, %d steps)"
+                  % (cells, T),
+        "value": t_both,
+        "unit": "s",
+        "higher_is_better": False,
+        "forward_s": t_fwd,
+        "reverse_s": t_both - t_fwd,
+        "reverse_cg_iterations": rinfo.reported_iterations,
+        "loss": loss,
+        "loss_forward_only": loss0,
+        "fd_directional": {"h": h, "direction": "density * (+-1, seeded)", "fd": fd_dir, "adjoint": g_dir,
+                           "rel_err": abs(fd_dir - g_dir) / abs(g_dir)},
+        "fd_cells": {"h_rel": 1e-3, "stencil": "4th-order central", "selection": "seeded, |g| >= 0.1 max|g|",
+                     "max_rel_err": max(x["rel_err"] for x in per_cell), "cells": per_cell},
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "adjoint problem: %dx%d cells, 8 rectangles (seed 4), reciprocal-density keyword, "
+                               "dt 0.004, %d FP64 CG steps at tl_eps 1e-15, per-step u checkpoints" % (cells, cells, T)},
+    }
+    print(json.dumps(out), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -281,6 +358,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.adjoint:
+        run_adjoint(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

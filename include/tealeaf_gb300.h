@@ -242,6 +242,33 @@ int tl_tea_leaf(tl_ctx* ctx, const tl_solve_opts* opts, double dt, tl_solve_info
 /* Forget the saved eigenvalue estimates (the reference's 'first' flag becomes true). */
 int tl_reset_eigen(tl_ctx* ctx);
 
+/* ---- adjoint (no counterpart in the reference) --------------------------- */
+
+/* Reverse mode of a run of tea_leaf() time steps: gradients of a loss on the final u (and/or
+ * energy1) with respect to the density field and the initial energy1.  One step is
+ * b = energy1*density, A(density) u = b (A from Kx, Ky of tea_leaf_common_kernel.f90:75-152),
+ * energy1' = u/density (finalise).  The reverse step solves A lambda = u_bar with the FP64 CG
+ * solve (A is symmetric) and chains dA/dKx, dA/dKy through the face formula to density.
+ * The exact-solve gradient: the recorded solves are taken as converged.
+ *
+ * tl_adjoint_begin allocates a tape for up to max_steps steps: each step's input energy1
+ * (and its solution u when store_solutions = 1; otherwise the reverse sweep recomputes u
+ * from the input energy1 with the recorded options).  Calling it again clears the tape. */
+int tl_adjoint_begin(tl_ctx* ctx, int max_steps, int store_solutions);
+/* tl_tea_leaf on the current fields, recording the step on the tape (TL_ERR_STATE if no tape
+ * or the tape is full). */
+int tl_adjoint_record_step(tl_ctx* ctx, const tl_solve_opts* opts, double dt, tl_solve_info* info);
+/* Reverse sweep over the recorded steps.  u_bar: dL/du of the last step's solution, e_bar:
+ * dL/d energy1 after the last step (host arrays, x_cells x y_cells, row stride ld; either may be
+ * NULL for zero).  density_bar (required) and energy0_bar (NULL to skip) receive dL/d density
+ * and dL/d energy1 at the first recorded step's input.  info sums the reverse solves
+ * (reported_iterations, solve_seconds, kernel_launches).  The chunk's fields are left
+ * overwritten; the tape is kept (call again with another u_bar). */
+int tl_adjoint_backward(tl_ctx* ctx, const double* u_bar, const double* e_bar, int ld, double* density_bar,
+                        double* energy0_bar, tl_solve_info* info);
+/* Free the tape. */
+int tl_adjoint_end(tl_ctx* ctx);
+
 /* ---- profiling (the reference's profiler_on timers, definitions.f90:107-121) ---- */
 
 /* Enable (1) or disable (0) CUDA-event timing of every launch of the fused solver-loop

@@ -84,6 +84,13 @@ struct tl_ctx {
   MixFields mix{};
   MixState* mst = nullptr;
   MixState* mst_host = nullptr;
+  // adjoint tape (tl_adjoint_*): per recorded step its input energy1 (and, when storing
+  // solutions, its u), plus four work fields: rhs, rho_bar, e_bar, recomputed u
+  char* tape = nullptr;
+  int tape_max = 0, tape_n = 0, tape_store_u = 0;
+  std::vector<double> tape_dt;
+  std::vector<tl_solve_opts> tape_opts;
+  double* tape_field(int i) const { return reinterpret_cast<double*>(tape + (size_t)i * field_stride); }
 
   double* slot(int s) const { return reinterpret_cast<double*>(slab + (size_t)s * field_stride); }
   Reduce rd() const { return Reduce{partials, counter, st, hist_a, hist_b, ch_a, ch_b}; }
@@ -379,6 +386,7 @@ int tl_destroy(tl_ctx* c) {
   if (c->ev1) cudaEventDestroy(c->ev1);
   for (int i = 0; i < 3 * tl_ctx::BATCH; ++i)
     if (c->pev[i]) cudaEventDestroy(c->pev[i]);
+  cudaFree(c->tape);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return TL_OK;
@@ -896,14 +904,22 @@ struct Solver {
 
 }  // namespace
 
-extern "C" int tl_tea_leaf(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info) {
-  if (!c || !o || !info) return fail(TL_ERR_ARG, "tl_tea_leaf: null argument");
+namespace {
+
+int check_opts(const tl_ctx* c, const tl_solve_opts* o) {
   if (o->solver < TL_SOLVER_JACOBI || o->solver > TL_SOLVER_PPCG) return fail(TL_ERR_ARG, "tl_tea_leaf: bad solver");
   if (o->max_iters < 1) return fail(TL_ERR_ARG, "tl_tea_leaf: max_iters must be >= 1");
   if (o->precision != TL_PRECISION_FP64 && o->precision != TL_PRECISION_MIXED)
     return fail(TL_ERR_ARG, "tl_tea_leaf: unknown precision form");
   if (o->precision == TL_PRECISION_MIXED && (o->solver != TL_SOLVER_CG || c->g.precond != TL_PREC_NONE))
     return fail(TL_ERR_ARG, "tl_tea_leaf: the mixed-precision form is implemented for unpreconditioned CG");
+  return TL_OK;
+}
+
+// One implicit solve (tea_solve.f90:37-503).  rhs (device, context layout; FP64 form only):
+// solve A u = rhs from the initial guess u = rhs instead of A u = energy1 * density.
+// finalise: energy1 = u / density at the end (tea_leaf_kernel_finalise).
+int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, const double* rhs, bool finalise) {
   memset(info, 0, sizeof(*info));
   Solver S{c, o, o->solver == TL_SOLVER_CG, o->solver == TL_SOLVER_CHEBY, o->solver == TL_SOLVER_PPCG,
            o->solver == TL_SOLVER_JACOBI, {}, {}};
@@ -921,6 +937,10 @@ extern "C" int tl_tea_leaf(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solv
   c->g.ry = dt / (c->g.dy * c->g.dy);
   launch_init_faces(c->f, c->L, c->g, c->stream);
   launch_init_cells(c->f, c->L, c->g, false, c->stream);
+  if (rhs) {
+    launch_copy_interior(c->f.u0, rhs, c->L, c->stream);
+    launch_copy_interior(c->f.u, rhs, c->L, c->stream);
+  }
   if ((rc = do_halo(c, M(TL_FIELD_U), 1))) return rc;
   if (o->precision == TL_PRECISION_MIXED) return mixed_cg(c, o, info, launches0);
   LoopState& H = *c->st_host;
@@ -1120,8 +1140,10 @@ extern "C" int tl_tea_leaf(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solv
     if ((rc = reduce_result(c, &exact_error))) return rc;
     exact_error = std::sqrt(exact_error);
   }
-  launch_finalise(c->f, c->L, c->stream);
-  if ((rc = do_halo(c, M(TL_FIELD_ENERGY1), 1))) return rc;
+  if (finalise) {
+    launch_finalise(c->f, c->L, c->stream);
+    if ((rc = do_halo(c, M(TL_FIELD_ENERGY1), 1))) return rc;
+  }
   if ((rc = check_launch("finalise"))) return rc;
   CK(cudaEventRecord(c->ev1, c->stream));
   CK(cudaStreamSynchronize(c->stream));
@@ -1141,5 +1163,135 @@ extern "C" int tl_tea_leaf(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solv
   info->eigmax = c->eigmax;
   info->solve_seconds = ms * 1e-3;
   info->kernel_launches = launch_counter() - launches0;
+  return TL_OK;
+}
+
+}  // namespace
+
+extern "C" int tl_tea_leaf(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info) {
+  if (!c || !o || !info) return fail(TL_ERR_ARG, "tl_tea_leaf: null argument");
+  int rc;
+  if ((rc = check_opts(c, o))) return rc;
+  return solve(c, o, dt, info, nullptr, true);
+}
+
+// ===========================================================================
+// Adjoint of a run of time steps (tl_adjoint.cu has the kernels)
+// ===========================================================================
+extern "C" int tl_adjoint_begin(tl_ctx* c, int max_steps, int store_solutions) {
+  if (!c) return fail(TL_ERR_ARG, "tl_adjoint_begin: null context");
+  if (max_steps < 1) return fail(TL_ERR_ARG, "tl_adjoint_begin: max_steps must be >= 1");
+  if (store_solutions != 0 && store_solutions != 1) return fail(TL_ERR_ARG, "tl_adjoint_begin: store_solutions is 0 or 1");
+  CK(cudaStreamSynchronize(c->stream));
+  cudaFree(c->tape);
+  c->tape = nullptr;
+  c->tape_max = c->tape_n = 0;
+  const size_t nf = (size_t)max_steps * (1 + store_solutions) + 4;
+  if (cudaMalloc(&c->tape, nf * c->field_stride) != cudaSuccess) {
+    cudaGetLastError();
+    c->tape = nullptr;
+    return fail(TL_ERR_ALLOC, "tl_adjoint_begin: cannot allocate the checkpoint fields");
+  }
+  CK(cudaMemsetAsync(c->tape, 0, nf * c->field_stride, c->stream));
+  c->tape_max = max_steps;
+  c->tape_store_u = store_solutions;
+  c->tape_dt.assign(max_steps, 0.0);
+  c->tape_opts.assign(max_steps, tl_solve_opts{});
+  return TL_OK;
+}
+
+extern "C" int tl_adjoint_record_step(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info) {
+  if (!c || !o || !info) return fail(TL_ERR_ARG, "tl_adjoint_record_step: null argument");
+  if (!c->tape) return fail(TL_ERR_STATE, "tl_adjoint_record_step: no tape (call tl_adjoint_begin)");
+  if (c->tape_n >= c->tape_max) return fail(TL_ERR_STATE, "tl_adjoint_record_step: tape full");
+  int rc;
+  if ((rc = check_opts(c, o))) return rc;
+  const size_t fb = (size_t)c->L.elems() * sizeof(double);
+  const int t = c->tape_n;
+  CK(cudaMemcpyAsync(c->tape_field(t), c->f.energy1, fb, cudaMemcpyDeviceToDevice, c->stream));
+  if ((rc = solve(c, o, dt, info, nullptr, true))) return rc;
+  if (c->tape_store_u)
+    CK(cudaMemcpyAsync(c->tape_field(c->tape_max + t), c->f.u, fb, cudaMemcpyDeviceToDevice, c->stream));
+  c->tape_dt[t] = dt;
+  c->tape_opts[t] = *o;
+  c->tape_n = t + 1;
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+extern "C" int tl_adjoint_backward(tl_ctx* c, const double* u_bar, const double* e_bar, int ld, double* density_bar,
+                                   double* energy0_bar, tl_solve_info* info) {
+  if (!c || !density_bar || !info) return fail(TL_ERR_ARG, "tl_adjoint_backward: null argument");
+  if (ld < c->L.nx) return fail(TL_ERR_ARG, "tl_adjoint_backward: ld < x_cells");
+  if (!c->tape || c->tape_n < 1) return fail(TL_ERR_STATE, "tl_adjoint_backward: no recorded steps");
+  const Layout& L = c->L;
+  const size_t fb = (size_t)L.elems() * sizeof(double);
+  const int T = c->tape_n, base = c->tape_max * (1 + c->tape_store_u);
+  double* rhs = c->tape_field(base);
+  double* rho_bar = c->tape_field(base + 1);
+  double* eb = c->tape_field(base + 2);
+  double* u_re = c->tape_field(base + 3);
+  const size_t row = sizeof(double) * L.nx, dpitch = sizeof(double) * L.ld, spitch = sizeof(double) * ld;
+  CK(cudaMemsetAsync(rhs, 0, fb, c->stream));
+  CK(cudaMemsetAsync(rho_bar, 0, fb, c->stream));
+  CK(cudaMemsetAsync(eb, 0, fb, c->stream));
+  if (u_bar)
+    CK(cudaMemcpy2DAsync(rhs + L.at(1, 1), dpitch, u_bar, spitch, row, L.ny, cudaMemcpyHostToDevice, c->stream));
+  if (e_bar)
+    CK(cudaMemcpy2DAsync(eb + L.at(1, 1), dpitch, e_bar, spitch, row, L.ny, cudaMemcpyHostToDevice, c->stream));
+  tl_solve_info total{}, one{};
+  int rc;
+  for (int t = T - 1; t >= 0; --t) {
+    const double* e_t = c->tape_field(t);
+    const double* u_t;
+    if (c->tape_store_u) {
+      u_t = c->tape_field(c->tape_max + t);
+    } else {
+      // recompute the step's solution from its checkpointed input energy
+      CK(cudaMemcpyAsync(c->f.energy1, e_t, fb, cudaMemcpyDeviceToDevice, c->stream));
+      if ((rc = solve(c, &c->tape_opts[t], c->tape_dt[t], &one, nullptr, true))) return rc;
+      CK(cudaMemcpyAsync(u_re, c->f.u, fb, cudaMemcpyDeviceToDevice, c->stream));
+      total.solve_seconds += one.solve_seconds;
+      total.kernel_launches += one.kernel_launches;
+      u_t = u_re;
+    }
+    // u_bar of this step: the loss term (last step only) plus e'_bar / rho
+    launch_adj_rhs(t == T - 1 ? rhs : nullptr, eb, u_t, c->f.density, rhs, rho_bar, L, c->stream);
+    // lambda = A^-1 u_bar by the FP64 CG solve (A is symmetric); lambda = 0 for u_bar = 0
+    double nrm = 0.0;
+    launch_norm2(rhs, L, c->rd(), RED_STORE, c->stream);
+    if ((rc = check_launch("adjoint rhs"))) return rc;
+    if ((rc = reduce_result(c, &nrm))) return rc;
+    if (nrm > 0.0) {
+      tl_solve_opts oc = c->tape_opts[t];
+      oc.solver = TL_SOLVER_CG;
+      oc.precision = TL_PRECISION_FP64;
+      if ((rc = solve(c, &oc, c->tape_dt[t], &one, rhs, false))) return rc;
+      total.reported_iterations += one.reported_iterations;
+      total.solve_seconds += one.solve_seconds;
+      total.kernel_launches += one.kernel_launches;
+    } else {
+      CK(cudaMemsetAsync(c->f.u, 0, fb, c->stream));
+    }
+    const double rx = c->tape_dt[t] / (c->g.dx * c->g.dx), ry = c->tape_dt[t] / (c->g.dy * c->g.dy);
+    launch_adj_accumulate(c->f.u, u_t, e_t, c->f.density, rho_bar, eb, L, rx, ry, c->g.coefficient, c->stream);
+    total.kernel_launches += 1;
+    if ((rc = check_launch("adjoint step"))) return rc;
+  }
+  CK(cudaMemcpy2DAsync(density_bar, spitch, rho_bar + L.at(1, 1), dpitch, row, L.ny, cudaMemcpyDeviceToHost,
+                       c->stream));
+  if (energy0_bar)
+    CK(cudaMemcpy2DAsync(energy0_bar, spitch, eb + L.at(1, 1), dpitch, row, L.ny, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  *info = total;
+  return TL_OK;
+}
+
+extern "C" int tl_adjoint_end(tl_ctx* c) {
+  if (!c) return fail(TL_ERR_ARG, "tl_adjoint_end: null context");
+  CK(cudaStreamSynchronize(c->stream));
+  cudaFree(c->tape);
+  c->tape = nullptr;
+  c->tape_max = c->tape_n = 0;
   return TL_OK;
 }

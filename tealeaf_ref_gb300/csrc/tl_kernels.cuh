@@ -106,4 +106,12 @@ void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd,
 // accept the correction: u += d (FP64), d = 0
 void launch_mix_apply(const Fields& f, const MixFields& m, const Layout& L, cudaStream_t s);
 
+// ---- adjoint of a time step (tl_adjoint.cu) ----
+// rhs = u_bar_ext (nullable) + e_bar / rho;  rho_bar -= e_bar u / rho^2
+void launch_adj_rhs(const double* u_bar_ext, const double* e_bar, const double* u, const double* rho, double* rhs,
+                    double* rho_bar, const Layout& L, cudaStream_t s);
+// rho_bar += lambda e + dA/dK terms chained to rho;  e_bar = lambda rho
+void launch_adj_accumulate(const double* lam, const double* u, const double* e, const double* rho, double* rho_bar,
+                           double* e_bar, const Layout& L, double rx, double ry, int coefficient, cudaStream_t s);
+
 }  // namespace tl

@@ -101,6 +101,10 @@ SIGNATURES = {
     "tl_update_halo": (_I, [_P, _I, _I]),
     "tl_tea_leaf": (_I, [_P, C.POINTER(SolveOpts), _D, C.POINTER(SolveInfo)]),
     "tl_reset_eigen": (_I, [_P]),
+    "tl_adjoint_begin": (_I, [_P, _I, _I]),
+    "tl_adjoint_record_step": (_I, [_P, C.POINTER(SolveOpts), _D, C.POINTER(SolveInfo)]),
+    "tl_adjoint_backward": (_I, [_P, _DP, _DP, _I, _DP, _DP, C.POINTER(SolveInfo)]),
+    "tl_adjoint_end": (_I, [_P]),
     "tl_cg_calc_w_noalloc": (_I, [_I, _I, _I, _P, _P, _P, _P, _P, _D, _D, _DP]),
     "tl_profile": (_I, [_P, _I]),
     "tl_profile_read": (_I, [_P, _I, _DP, C.POINTER(C.c_longlong)]),
@@ -261,6 +265,41 @@ class Chunk:
         info = SolveInfo()
         _check(self.L.tl_tea_leaf(self.ptr, C.byref(o), dt, C.byref(info)))
         return info
+
+    # ---- adjoint (tl_adjoint_*) ----
+    def adjoint_begin(self, max_steps: int, store_solutions: bool = True) -> None:
+        _check(self.L.tl_adjoint_begin(self.ptr, max_steps, int(store_solutions)))
+
+    def record_step(self, deck_or_opts, dt: Optional[float] = None) -> SolveInfo:
+        """tea_leaf() for one time step, recorded on the adjoint tape."""
+        opts = deck_or_opts if isinstance(deck_or_opts, SolveOpts) else opts_from_deck(deck_or_opts)
+        if dt is None:
+            dt = deck_or_opts.initial_timestep
+        info = SolveInfo()
+        _check(self.L.tl_adjoint_record_step(self.ptr, C.byref(opts), dt, C.byref(info)))
+        return info
+
+    def adjoint_backward(self, u_bar: Optional[np.ndarray], e_bar: Optional[np.ndarray] = None,
+                         want_energy0: bool = True):
+        """(dL/d density, dL/d initial energy1 or None, SolveInfo of the reverse solves)."""
+        def arg(a):
+            if a is None:
+                return None, None
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            if a.shape != (self.ny, self.nx):
+                raise ValueError("expected shape (y_cells, x_cells)")
+            return a, _dp(a)
+        ub, ubp = arg(u_bar)
+        eb, ebp = arg(e_bar)
+        rho_bar = np.empty((self.ny, self.nx), dtype=np.float64)
+        e0_bar = np.empty((self.ny, self.nx), dtype=np.float64) if want_energy0 else None
+        info = SolveInfo()
+        _check(self.L.tl_adjoint_backward(self.ptr, ubp, ebp, self.nx, _dp(rho_bar),
+                                          _dp(e0_bar) if e0_bar is not None else None, C.byref(info)))
+        return rho_bar, e0_bar, info
+
+    def adjoint_end(self) -> None:
+        _check(self.L.tl_adjoint_end(self.ptr))
 
     def reset_eigen(self) -> None:
         _check(self.L.tl_reset_eigen(self.ptr))

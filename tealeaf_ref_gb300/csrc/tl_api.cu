@@ -882,6 +882,72 @@ struct Solver {
     return reduce_result(c, out);
   }
 
+  // Precision form: the inner steps in FP32 (tl_mixed_poly.cu), z = utemp in FP64.
+  int run_ppcg_inner_steps32(int inner_steps) {
+    if (inner_steps < 0) return TL_OK;
+    launch_poly_ppcg_inner(c->f, c->mix, c->L, c->theta, inner_steps, ch_a.data(), ch_b.data(), c->stream);
+    return check_launch("ppcg_inner_steps (FP32)");
+  }
+
+  // Chebyshev phase of the precision form, from the switch to the end of the solve: FP64
+  // refinement cycles, each an FP32 Chebyshev solve of A d = r (the FP64 residual of u,
+  // rounded) with the eigenvalue bounds and coefficients of the FP64 form, accepted (u += d in
+  // FP64) only if the FP64 residual of u + d is lower.  The cycle length makes the Chebyshev
+  // error bound fall by 1e-4 (gamma = (sqrt(cn)-1)/(sqrt(cn)+1), as est_itc uses).  Stops at
+  // the reference's test on the FP64 residual, at its rounding floor, on a rejected or
+  // stalled cycle, or when max_iters steps are used.  Returns the steps taken.
+  int run_mixed_cheby(int budget, double initial_residual, double* error, int* steps, int* stop) {
+    const Reduce rd = c->rd();
+    MixState& H = *c->mst_host;
+    const double gamma = (std::sqrt(c->cn) - 1.0) / (std::sqrt(c->cn) + 1.0);
+    int m = (gamma > 0.0 && gamma < 1.0) ? (int)std::ceil(std::log(1e-4) / std::log(gamma)) : 16;
+    m = std::max(8, std::min(m, (int)ch_a.size() - 1));
+    launch_poly_clear(c->mix, c->L, c->stream);
+    // the residual with u's halo as it stands (not exchanged after the switch)
+    launch_mix_trial(c->f, c->mix, c->L, rd, c->mst, false, c->stream, false);  // m.r = u0 - A u
+    int rc;
+    if ((rc = check_launch("mixed chebyshev residual"))) return rc;
+    if ((rc = sync_mix(c))) return rc;
+    double res = std::sqrt(std::fabs(H.trial_rr));
+    double floor_est = DBL_EPSILON * std::sqrt(H.trial_scale);
+    int total = 0, stalled = 0;
+    *stop = TL_STOP_CAP;
+    while (true) {
+      if (res < o->eps * initial_residual) {
+        *stop = TL_STOP_EPS;
+        break;
+      }
+      if (res <= TL_FLOOR_FACTOR * floor_est) {
+        *stop = TL_STOP_FLOOR;
+        break;
+      }
+      const int len = std::min(m, budget - total);
+      if (len < 1) break;
+      launch_poly_cheby(c->mix, c->L, c->theta, len, ch_a.data(), ch_b.data(), c->stream);
+      launch_mix_trial(c->f, c->mix, c->L, rd, c->mst, false, c->stream, false);  // m.r = u0 - A (u + d)
+      if ((rc = check_launch("mixed chebyshev cycle"))) return rc;
+      if ((rc = sync_mix(c))) return rc;
+      total += len;
+      const double res_t = std::sqrt(std::fabs(H.trial_rr));
+      if (!std::isfinite(res_t)) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite residual");
+      if (!(res_t < res)) {
+        *stop = TL_STOP_REJECT;  // d dropped; m.r already holds the residual of u + d, not needed
+        break;
+      }
+      launch_mix_apply(c->f, c->mix, c->L, c->stream);  // u += d (FP64), d = 0
+      stalled = (res_t > 0.5 * res) ? stalled + 1 : 0;
+      res = res_t;
+      floor_est = DBL_EPSILON * std::sqrt(H.trial_scale);
+      if (stalled >= 3) {
+        *stop = TL_STOP_STALL;
+        break;
+      }
+    }
+    *error = res;
+    *steps = total;
+    return check_launch("mixed chebyshev");
+  }
+
   int run_ppcg_inner_steps(int inner_steps) {
     // tea_leaf_ppcg.f90:211-431 on one chunk (every face external: bounds = interior)
     if (inner_steps < 0) return TL_OK;
@@ -911,8 +977,9 @@ int check_opts(const tl_ctx* c, const tl_solve_opts* o) {
   if (o->max_iters < 1) return fail(TL_ERR_ARG, "tl_tea_leaf: max_iters must be >= 1");
   if (o->precision != TL_PRECISION_FP64 && o->precision != TL_PRECISION_MIXED)
     return fail(TL_ERR_ARG, "tl_tea_leaf: unknown precision form");
-  if (o->precision == TL_PRECISION_MIXED && (o->solver != TL_SOLVER_CG || c->g.precond != TL_PREC_NONE))
-    return fail(TL_ERR_ARG, "tl_tea_leaf: the mixed-precision form is implemented for unpreconditioned CG");
+  if (o->precision == TL_PRECISION_MIXED && (o->solver == TL_SOLVER_JACOBI || c->g.precond != TL_PREC_NONE))
+    return fail(TL_ERR_ARG,
+                "tl_tea_leaf: the mixed-precision form is implemented for CG, Chebyshev and PPCG without preconditioner");
   return TL_OK;
 }
 
@@ -942,7 +1009,13 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
     launch_copy_interior(c->f.u, rhs, c->L, c->stream);
   }
   if ((rc = do_halo(c, M(TL_FIELD_U), 1))) return rc;
-  if (o->precision == TL_PRECISION_MIXED) return mixed_cg(c, o, info, launches0);
+  const bool mixed = o->precision == TL_PRECISION_MIXED;
+  if (mixed && S.use_cg) return mixed_cg(c, o, info, launches0);
+  if (mixed) {
+    // FP32 copies of the operator for the Chebyshev / PPCG polynomial sweeps
+    if ((rc = ensure_mix(c))) return rc;
+    launch_mix_prep(c->f, c->mix, c->L, c->stream);
+  }
   LoopState& H = *c->st_host;
   memset(&H, 0, sizeof(H));
   H.eps = o->eps;
@@ -1071,13 +1144,23 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
         c->cn = c->eigmax / c->eigmin;
         // p currently lives in whichever CG buffer the last iteration wrote; step 3 rebuilds p
         launch_ppcg_init(c->f, c->L, c->g, 2, ppcg_active, c->rd(), RED_STORE, c->stream);
-        if ((rc = S.run_ppcg_inner_steps(inner))) return rc;
+        if ((rc = mixed ? S.run_ppcg_inner_steps32(inner) : S.run_ppcg_inner_steps(inner))) return rc;
         ppcg_inner_iters += inner;
         launch_ppcg_init(c->f, c->L, c->g, 3, ppcg_active, c->rd(), RED_STORE, c->stream);
         if ((rc = check_launch("ppcg_init"))) return rc;
         if ((rc = reduce_result(c, &rro))) return rc;
         fields_mask = M(TL_FIELD_P);
         if ((rc = do_halo(c, fields_mask, 1))) return rc;
+      }
+      if (S.use_cheby && mixed) {
+        int steps = 0, stop = 0;
+        if ((rc = S.run_mixed_cheby(max_iters - n + 1, initial_residual, &error, &steps, &stop))) return rc;
+        cheby_calc_steps = steps;
+        n += steps;
+        info->stop_reason = stop;
+        info->true_residual = error;
+        exited = true;
+        break;
       }
       if (S.use_cheby) {
         if (cheby_calc_steps == 0) {
@@ -1106,7 +1189,7 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
         if ((rc = reduce_result(c, &rro))) return rc;
         const double alpha = rro / pw;
         launch_cg_calc_ur(c->f, c->L, c->g, alpha, c->rd(), c->stream);
-        if ((rc = S.run_ppcg_inner_steps(inner))) return rc;
+        if ((rc = mixed ? S.run_ppcg_inner_steps32(inner) : S.run_ppcg_inner_steps(inner))) return rc;
         ppcg_inner_iters += inner;
         launch_dot(c->f.z, c->f.r, c->f.r_store, c->L, c->rd(), RED_STORE, c->stream);
         if ((rc = reduce_result(c, &rrn))) return rc;

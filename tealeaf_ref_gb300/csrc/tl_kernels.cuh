@@ -99,12 +99,25 @@ struct MixState {
 void launch_mix_prep(const Fields& f, const MixFields& m, const Layout& L, cudaStream_t s);
 // d += alpha p if an update is pending (the host clears MixState::d_pending afterwards)
 void launch_mix_flush_d(const MixFields& m, const Layout& L, MixState* ms, cudaStream_t s);
-// trial residual r = u0 - A (u + d) in FP64 (u unchanged), r32 = r; first: also p32 = r
+// trial residual r = u0 - A (u + d) in FP64 (u unchanged), r32 = r; first: also p32 = r.
+// mirror: off-domain neighbours mirrored (CG); else read from the halo cells (Chebyshev)
 void launch_mix_trial(const Fields& f, const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms,
-                      bool first, cudaStream_t s);
+                      bool first, cudaStream_t s, bool mirror = true);
 void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms, cudaStream_t s);
 // accept the correction: u += d (FP64), d = 0
 void launch_mix_apply(const Fields& f, const MixFields& m, const Layout& L, cudaStream_t s);
+
+// ---- FP32 polynomial sweeps of the precision form of Chebyshev / PPCG (tl_mixed_poly.cu) ----
+// PPCG inner loop in FP32 from the FP64 r: inner_steps Chebyshev steps with ch_a/ch_b[1..],
+// z (FP64) = utemp at the end
+void launch_poly_ppcg_inner(const Fields& f, const MixFields& m, const Layout& L, double theta, int inner_steps,
+                            const double* ch_a, const double* ch_b, cudaStream_t s);
+// `steps` Chebyshev steps (start + steps-1 iterations with ch_a/ch_b[1..]) on A d = m.r from
+// d = 0; d ends in m.d
+void launch_poly_cheby(const MixFields& m, const Layout& L, double theta, int steps, const double* ch_a,
+                       const double* ch_b, cudaStream_t s);
+// m.d = m.p2 = 0
+void launch_poly_clear(const MixFields& m, const Layout& L, cudaStream_t s);
 
 // ---- adjoint of a time step (tl_adjoint.cu) ----
 // rhs = u_bar_ext (nullable) + e_bar / rho;  rho_bar -= e_bar u / rho^2

@@ -118,16 +118,19 @@ __global__ void k_mix_prep(Fields f, MixFields m, Layout L) {
 // and of the residual arithmetic leaves r uncertain by a small multiple of eps_64 times it,
 // the level below which no correction can lower the true residual.
 // first: the start of the CG process, p32 = r32 in the buffer the next k_mix_w reads as its
-// previous direction.
-__global__ void k_mix_trial(Fields f, MixFields m, Layout L, Reduce rd, MixState* ms, bool first) {
+// previous direction.  mirror = false: off-domain neighbours are read from the halo cells as
+// they are (u's halo as last exchanged, d's halo zero) -- the operator the reference's
+// Chebyshev iteration applies, whose u halo is not exchanged after the switch
+// (tea_solve.f90:246-250).
+__global__ void k_mix_trial(Fields f, MixFields m, Layout L, Reduce rd, MixState* ms, bool first, bool mirror) {
   double acc[3] = {0.0, 0.0, 0.0};
   float* __restrict__ p0 = (ms->n & 1) ? m.p : m.p2;
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
     if (j > L.nx) continue;
     const long long c = L.at(j, k);
-    const long long cl = (j > 1) ? c - 1 : c, cr = (j < L.nx) ? c + 1 : c;
-    const long long cb = (k > 1) ? c - L.ld : c, ct = (k < L.ny) ? c + L.ld : c;
+    const long long cl = (j > 1 || !mirror) ? c - 1 : c, cr = (j < L.nx || !mirror) ? c + 1 : c;
+    const long long cb = (k > 1 || !mirror) ? c - L.ld : c, ct = (k < L.ny || !mirror) ? c + L.ld : c;
     const double uc = f.u[c] + (double)m.d[c];
     const double ul = f.u[cl] + (double)m.d[cl], ur = f.u[cr] + (double)m.d[cr];
     const double ub = f.u[cb] + (double)m.d[cb], ut = f.u[ct] + (double)m.d[ct];
@@ -337,9 +340,9 @@ void launch_mix_prep(const Fields& f, const MixFields& m, const Layout& L, cudaS
 }
 
 void launch_mix_trial(const Fields& f, const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms,
-                      bool first, cudaStream_t s) {
+                      bool first, cudaStream_t s, bool mirror) {
   dim3 grid((L.nx + 255) / 256, L.ny < 256 ? L.ny : 256);
-  { ++launch_counter(); k_mix_trial<<<grid, 256, 0, s>>>(f, m, L, rd, ms, first); }
+  { ++launch_counter(); k_mix_trial<<<grid, 256, 0, s>>>(f, m, L, rd, ms, first, mirror); }
 }
 
 void launch_mix_flush_d(const MixFields& m, const Layout& L, MixState* ms, cudaStream_t s) {

@@ -82,11 +82,66 @@ def test_mixed_cg_reference_deck(golden):
     assert _rel(s, ref) < 1e-10
 
 
-def test_mixed_rejected_for_other_solvers():
+POLY_CASES = [
+    dict(solver="ppcg", ppcg_inner_steps=10, ch_cg_presteps=20),
+    dict(solver="ppcg", ppcg_inner_steps=10, ch_cg_presteps=20, coefficient=1),
+    dict(solver="ppcg", ppcg_inner_steps=8, ch_cg_presteps=20, reflective=True),
+    dict(solver="ppcg", ppcg_inner_steps=5, ch_cg_presteps=20, nx=131, ny=77),
+    dict(solver="chebyshev", ch_cg_presteps=20),
+    dict(solver="chebyshev", ch_cg_presteps=20, coefficient=1),
+    dict(solver="chebyshev", ch_cg_presteps=20, reflective=True),
+    dict(solver="chebyshev", ch_cg_presteps=30, nx=131, ny=77),
+]
+
+
+@pytest.mark.parametrize("case", POLY_CASES, ids=["-".join("%s%s" % kv for kv in c.items()) for c in POLY_CASES])
+def test_mixed_chebyshev_ppcg_match_fp64_oracle(case):
+    """FP32 inner sweeps (PPCG's preconditioner steps; Chebyshev iterations on a correction in FP64
+    refinement) against the FP64 oracle at the FP64 form's bars."""
+    from oracle import oracle
     from tealeaf_ref_gb300 import native
 
-    d = small_deck(nx=16, ny=16, solver="ppcg", ppcg_inner_steps=4)
+    kw = dict(nx=67, ny=45, steps=3, n_rect=4, n_circ=2, max_iters=20000)
+    kw.update(case)
+    d = small_deck(**kw)
+    ro = oracle.run_deck(d)
+    opts = native.opts_from_deck(d, precision="mixed")
     with native.Chunk.from_deck(d) as c:
-        with pytest.raises(native.TeaLeafError) as e:
-            c.tea_leaf(native.opts_from_deck(d, precision="mixed"), d.initial_timestep)
-        assert e.value.code == -1
+        infos = [c.tea_leaf(opts, d.initial_timestep) for _ in range(d.end_step)]
+        s = c.field_summary()
+        u = c.download("u")
+    o = oracle.Chunk.from_deck(d)
+    for _ in range(d.end_step):
+        o.tea_leaf(d)
+    assert _rel(s, ro.summaries[-1][1]) < 1e-10
+    assert _rel(u, np.array(o.interior("u"))) < 1e-8
+    for i in infos:
+        assert i.reported_iterations < d.max_iters
+        if d.solver == "chebyshev":
+            assert native.STOP_REASONS[i.stop_reason] in ("eps", "floor", "stall", "reject")
+            assert i.true_residual <= 1e-9 * i.initial_residual
+
+
+def test_mixed_ppcg_reference_deck(golden):
+    """The reference's tea.in (PPCG, 1000^2, halo depth 2, test problem 4) in the mixed form:
+    the reference's QA temperature (its own 1e-5 bar) and the FP64 form's summary (1e-10)."""
+    from tealeaf_ref_gb300 import native
+
+    d = dk.parse_deck(golden["ppcg_deck"])
+    r64 = native.run_deck(d)
+    rmx = native.run_deck(d, precision="mixed")
+    assert _rel(rmx.summaries[-1][1], r64.summaries[-1][1]) < 1e-10
+    qa = float(golden["qa_temperature"]["4"])
+    assert abs(rmx.summaries[-1][1][3] - qa) <= 1e-5 * abs(qa)
+
+
+def test_mixed_rejected_for_jacobi_and_preconditioners():
+    from tealeaf_ref_gb300 import native
+
+    for kw in (dict(solver="jacobi"), dict(solver="cg", precond="jac_diag"),
+               dict(solver="ppcg", ppcg_inner_steps=4, precond="jac_block")):
+        d = small_deck(nx=16, ny=16, **kw)
+        with native.Chunk.from_deck(d) as c:
+            with pytest.raises(native.TeaLeafError) as e:
+                c.tea_leaf(native.opts_from_deck(d, precision="mixed"), d.initial_timestep)
+            assert e.value.code == -1

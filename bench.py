@@ -67,6 +67,11 @@ def parse():
                     help="instead of the CG line: the adjoint problem (2048^2, 10 steps; gradient of "
                          "sum (u - u_target)^2 wrt density), forward + reverse time and finite-difference checks")
     ap.add_argument("--fd-cells", type=int, default=8, help="adjoint: cells for the per-cell difference check")
+    ap.add_argument("--solver", default="cg", choices=["cg", "jacobi", "chebyshev", "ppcg"],
+                    help="jacobi / chebyshev / ppcg: instead of the CG line, time steps of that solver on the "
+                         "4096^2 workloads (Jacobi: 8 rectangles, seed 2, capped at --iters; Chebyshev / PPCG: "
+                         "seed 3, 20 CG presteps, PPCG 10 inner steps, solved to tl_eps) and report per-kernel "
+                         "GB/s from a separately profiled step")
     return ap.parse_args()
 
 
@@ -320,6 +325,85 @@ def run_adjoint(args):
     print(json.dumps(out), flush=True)
 
 
+# Compulsory bytes per cell of one launch (or one step) of each timed kernel: FP64 Chebyshev
+# iterate 56 B (u, u0, p, Kx, Ky read; p, u written), PPCG inner step 64 B (sd, rtemp, utemp,
+# Kx, Ky read; sd, rtemp, utemp written), Jacobi 40 B (u0, un, Kx, Ky read; u written); the
+# FP32 forms at 4 B per stream: PPCG inner step 32 B, Chebyshev step on a correction 28 B
+# (d, r, p, Kx, Ky read; p, d written); FP32 CG sweeps 32 B (r, p_old, Kx, Ky, d read; p, w, d
+# written) and 12 B (w, r read; r written).
+KERNEL_BYTES = {"cheby_iterate": 56, "ppcg_inner": 64, "jacobi": 40, "mix_matvec": 32, "mix_update": 12,
+                "cg_matvec": 64, "cg_update": 24}
+POLY_BYTES = {"ppcg": 32, "chebyshev": 28}
+
+
+def run_solver(args):
+    """Time steps of the Jacobi, Chebyshev or PPCG solver (FP64 or mixed form) on the 4096^2
+    workloads; per-kernel times come from one more step run with the kernel timers on (the
+    host-driven loops wait for each timed launch, so that step is not part of the timing)."""
+    from tealeaf_ref_gb300 import deck as dk
+    from tealeaf_ref_gb300 import native
+
+    cells_n = args.cells if args.cells != 8192 else 4096
+    if args.solver == "jacobi":
+        d = dk.config_deck(2, solver="jacobi", cells=cells_n)
+        d.max_iters = args.iters
+    else:
+        d = dk.config_deck(3, solver=args.solver, cells=cells_n)
+        d.ch_cg_presteps = 20
+    opts = native.opts_from_deck(d, args.precision)
+    dt = d.initial_timestep
+    cells = cells_n * cells_n
+    with native.Chunk.from_deck(d) as c:
+        for _ in range(args.warmup):
+            c.tea_leaf(opts, dt)
+        infos = []
+        with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+            for _ in range(args.steps):
+                infos.append(c.tea_leaf(opts, dt))
+        dev_s = sum(i.solve_seconds for i in infos)
+        c.profile(True)
+        pinfo = c.tea_leaf(opts, dt)
+        kernels = {}
+        for name, kid in native.KERNEL_TIMERS.items():
+            ms, n = c.profile_read(name)
+            if not n:
+                continue
+            basis = (POLY_BYTES[args.solver] if name == "poly_step" else KERNEL_BYTES[name])
+            avg = ms / n * 1e-3
+            kernels[name] = {"launches": n, "ms_avg": 1e3 * avg, "bytes_per_cell": basis,
+                             "gbs": basis * cells / avg / 1e9}
+        c.profile(False)
+    peak, peak_kind = measured_peaks()
+    for k in kernels.values():
+        k["frac_of_peak"] = k["gbs"] / peak
+    out = {
+        "metric": "%s time per time step (%s, %d^2)" % (args.solver, args.precision, cells_n),
+        "value": dev_s / args.steps,
+        "unit": "s",
+        "higher_is_better": False,
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "iterations_per_step": [i.reported_iterations for i in infos],
+        "ppcg_inner_per_step": [i.ppcg_inner_iters for i in infos],
+        "cg_presteps_per_step": [i.cg_calc_steps for i in infos],
+        "cell_iterations_per_s": cells * sum(i.reported_iterations for i in infos) / dev_s,
+        "kernels": kernels,
+        "peak_gbs": peak,
+        "peak_source": peak_kind,
+        "profiled_step_iterations": pinfo.reported_iterations,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic",
+        "clocks": clk.summary(),
+        "config": {"workload": "TeaLeaf implicit diffusion, %s (%s), %dx%d cells, 8 rectangles, reciprocal-density "
+                               "keyword, dt 0.004, tl_eps 1e-15%s" % (
+                                   args.solver, args.precision, cells_n, cells_n,
+                                   ", capped at %d iterations" % args.iters if args.solver == "jacobi" else
+                                   ", 20 CG presteps" + (", 10 PPCG inner steps" if args.solver == "ppcg" else ""))},
+    }
+    print(json.dumps(out), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -361,6 +445,9 @@ def main():
         return
     if args.adjoint:
         run_adjoint(args)
+        return
+    if args.solver != "cg":
+        run_solver(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

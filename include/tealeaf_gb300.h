@@ -83,10 +83,13 @@ typedef struct tl_solve_opts {
   int ppcg_inner_steps;  /* tl_ppcg_inner_steps (after the PPCG default) */
   int check_result;      /* tl_check_result */
   /* Precision form (no reference counterpart): TL_PRECISION_FP64 runs the reference's
-   * algorithm in FP64; TL_PRECISION_MIXED (unpreconditioned CG) runs CG on FP32 vectors and
-   * FP32 copies of the operator, with FP64 reductions and step coefficients, the solution
-   * accumulated in FP64 and the residual periodically replaced by the FP64 true residual
-   * u0 - A u (the CG search direction is kept across replacements). */
+   * algorithm in FP64.  TL_PRECISION_MIXED (CG, Chebyshev, PPCG; no preconditioner):
+   * CG runs on FP32 vectors and FP32 copies of the operator, with FP64 reductions and step
+   * coefficients, the solution accumulated in FP64 and the residual periodically replaced by
+   * the FP64 true residual u0 - A u (the search direction is kept across replacements);
+   * PPCG runs its inner Chebyshev steps in FP32 inside the FP64 outer iteration; Chebyshev,
+   * after its FP64 CG presteps, runs FP32 Chebyshev cycles on the correction inside FP64
+   * iterative refinement. */
   int precision;
   double inner_tol;      /* mixed: replace the residual each time it has fallen by this
                             factor since the last replacement (0: 0.5) */
@@ -126,9 +129,16 @@ typedef struct tl_solve_info {
 #define TL_FLOOR_FACTOR 16.0
 
 /* Kernel ids for the per-kernel timers (tl_profile_read). */
-#define TL_KERNEL_CG_MATVEC 0 /* fused p update + w = A p + p.w sweep of the CG loop */
-#define TL_KERNEL_CG_UPDATE 1 /* fused u, r update + r.r sweep of the CG loop */
-#define TL_NUM_KERNEL_TIMERS 2
+#define TL_KERNEL_CG_MATVEC 0     /* fused p update + w = A p + p.w sweep of the CG loop */
+#define TL_KERNEL_CG_UPDATE 1     /* fused u, r update + r.r sweep of the CG loop */
+#define TL_KERNEL_CHEBY_ITERATE 2 /* Chebyshev iteration (tea_leaf_kernel_cheby_iterate), FP64 form */
+#define TL_KERNEL_PPCG_INNER 3    /* one PPCG inner step (tea_leaf_kernel_ppcg_inner), FP64 form */
+#define TL_KERNEL_JACOBI 4        /* Jacobi sweep with its L1 error (tea_leaf_jacobi_solve_kernel) */
+#define TL_KERNEL_MIX_MATVEC 5    /* mixed CG: FP32 p update + w = A p + p.w sweep */
+#define TL_KERNEL_MIX_UPDATE 6    /* mixed CG: FP32 r update + r.r sweep */
+#define TL_KERNEL_POLY_STEP 7     /* mixed Chebyshev / PPCG: one FP32 polynomial step (the time of a
+                                     block of steps, its set-up included, per step) */
+#define TL_NUM_KERNEL_TIMERS 8
 
 /* ---- context ----------------------------------------------------------- */
 
@@ -271,8 +281,10 @@ int tl_adjoint_end(tl_ctx* ctx);
 
 /* ---- profiling (the reference's profiler_on timers, definitions.f90:107-121) ---- */
 
-/* Enable (1) or disable (0) CUDA-event timing of every launch of the fused solver-loop
- * kernels on the context's stream; enabling also clears the accumulated totals. */
+/* Enable (1) or disable (0) CUDA-event timing of every launch of the solver-loop kernels
+ * (TL_KERNEL_*) on the context's stream; enabling also clears the accumulated totals.  The
+ * host-driven loops (Chebyshev, PPCG, Jacobi) wait for each timed launch, which adds launch
+ * gaps to the solve time while timing is on. */
 int tl_profile(tl_ctx* ctx, int enable);
 /* Accumulated device time (ms) and launch count of one TL_KERNEL_* since tl_profile(ctx,1). */
 int tl_profile_read(tl_ctx* ctx, int kernel_id, double* total_ms, long long* launches);

@@ -76,6 +76,7 @@ struct tl_ctx {
   static constexpr int BATCH = 16;
   bool prof = false;
   cudaEvent_t pev[3 * BATCH] = {};
+  cudaEvent_t qe0 = nullptr, qe1 = nullptr;  // one timed launch of a host-driven loop
   double prof_ms[TL_NUM_KERNEL_TIMERS] = {};
   long long prof_n[TL_NUM_KERNEL_TIMERS] = {};
   long long nlaunch = 0;  // kernels launched by the current tl_tea_leaf call
@@ -172,6 +173,23 @@ int ensure_ch(tl_ctx* c, int n) {
   CK(cudaMalloc(&c->ch_a, sizeof(double) * n));
   CK(cudaMalloc(&c->ch_b, sizeof(double) * n));
   c->ch_cap = n;
+  return TL_OK;
+}
+
+// Timers of the host-driven loops: prof_begin before a launch, prof_end after it waits for it
+// and adds its time to TL_KERNEL id (count units).  No-ops unless tl_profile is on.
+int prof_begin(tl_ctx* c) {
+  if (c->prof) CK(cudaEventRecord(c->qe0, c->stream));
+  return TL_OK;
+}
+int prof_end(tl_ctx* c, int id, int count) {
+  if (!c->prof) return TL_OK;
+  CK(cudaEventRecord(c->qe1, c->stream));
+  CK(cudaEventSynchronize(c->qe1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->qe0, c->qe1));
+  c->prof_ms[id] += ms;
+  c->prof_n[id] += count;
   return TL_OK;
 }
 
@@ -327,6 +345,8 @@ int tl_create(int x_cells, int y_cells, int halo_depth, int coefficient, int pre
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
   for (int i = 0; i < 3 * tl_ctx::BATCH && e == cudaSuccess; ++i) e = cudaEventCreate(&c->pev[i]);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->qe0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->qe1);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) {
     int rc = (e == cudaErrorMemoryAllocation) ? TL_ERR_ALLOC : TL_ERR_CUDA;
@@ -386,6 +406,8 @@ int tl_destroy(tl_ctx* c) {
   if (c->ev1) cudaEventDestroy(c->ev1);
   for (int i = 0; i < 3 * tl_ctx::BATCH; ++i)
     if (c->pev[i]) cudaEventDestroy(c->pev[i]);
+  if (c->qe0) cudaEventDestroy(c->qe0);
+  if (c->qe1) cudaEventDestroy(c->qe1);
   cudaFree(c->tape);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -789,9 +811,26 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
     H.phase_end = 0x7fffffff;
     CK(cudaMemcpyAsync(c->mst, &H, sizeof(MixState), cudaMemcpyHostToDevice, c->stream));
     while (H.status == RUN) {
-      for (int i = 0; i < batch; ++i) launch_mix_iteration(c->mix, c->L, rd, c->mst, c->stream);
+      const int n_before = H.n;
+      for (int i = 0; i < batch; ++i) {
+        if (c->prof) CK(cudaEventRecord(c->pev[3 * i], c->stream));
+        launch_mix_iteration(c->mix, c->L, rd, c->mst, c->stream, c->prof ? c->pev[3 * i + 1] : nullptr);
+        if (c->prof) CK(cudaEventRecord(c->pev[3 * i + 2], c->stream));
+      }
       if ((rc = check_launch("mixed batch"))) return rc;
       if ((rc = sync_mix(c))) return rc;
+      if (c->prof) {
+        const int ran = std::min(std::max(H.n - n_before, 0), batch);
+        for (int i = 0; i < ran; ++i) {
+          float a = 0.f, b = 0.f;
+          CK(cudaEventElapsedTime(&a, c->pev[3 * i], c->pev[3 * i + 1]));
+          CK(cudaEventElapsedTime(&b, c->pev[3 * i + 1], c->pev[3 * i + 2]));
+          c->prof_ms[TL_KERNEL_MIX_MATVEC] += a;
+          c->prof_ms[TL_KERNEL_MIX_UPDATE] += b;
+        }
+        c->prof_n[TL_KERNEL_MIX_MATVEC] += ran;
+        c->prof_n[TL_KERNEL_MIX_UPDATE] += ran;
+      }
     }
     if (H.status == EXIT_BREAKDOWN) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite FP32 CG scalar");
     const bool capped = H.n > H.max_n;
@@ -885,7 +924,10 @@ struct Solver {
   // Precision form: the inner steps in FP32 (tl_mixed_poly.cu), z = utemp in FP64.
   int run_ppcg_inner_steps32(int inner_steps) {
     if (inner_steps < 0) return TL_OK;
+    int rc;
+    if ((rc = prof_begin(c))) return rc;
     launch_poly_ppcg_inner(c->f, c->mix, c->L, c->theta, inner_steps, ch_a.data(), ch_b.data(), c->stream);
+    if ((rc = prof_end(c, TL_KERNEL_POLY_STEP, std::max(inner_steps, 1)))) return rc;
     return check_launch("ppcg_inner_steps (FP32)");
   }
 
@@ -923,7 +965,9 @@ struct Solver {
       }
       const int len = std::min(m, budget - total);
       if (len < 1) break;
+      if ((rc = prof_begin(c))) return rc;
       launch_poly_cheby(c->mix, c->L, c->theta, len, ch_a.data(), ch_b.data(), c->stream);
+      if ((rc = prof_end(c, TL_KERNEL_POLY_STEP, len))) return rc;
       launch_mix_trial(c->f, c->mix, c->L, rd, c->mst, false, c->stream, false);  // m.r = u0 - A (u + d)
       if ((rc = check_launch("mixed chebyshev cycle"))) return rc;
       if ((rc = sync_mix(c))) return rc;
@@ -958,7 +1002,9 @@ struct Solver {
       if ((rc = do_halo(c, M(TL_FIELD_SD) | M(TL_FIELD_R), h))) return rc;
       for (int be = h - 1; be >= 0; --be) {
         const int step = cur + h - 1 - be;
+        if ((rc = prof_begin(c))) return rc;
         launch_ppcg_inner(c->f, c->L, c->g, ch_a[step], ch_b[step], c->stream);
+        if ((rc = prof_end(c, TL_KERNEL_PPCG_INNER, 1))) return rc;
         if (c->g.reflective && (rc = do_halo(c, M(TL_FIELD_SD), 1))) return rc;
         if (step == inner_steps) break;
       }
@@ -1168,14 +1214,18 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
           if ((rc = S.norm(c->f.u0, &bb))) return rc;
           launch_cheby_init(c->f, c->L, c->g, c->theta, c->stream);
           if ((rc = do_halo(c, fields_mask, 1))) return rc;
+          if ((rc = prof_begin(c))) return rc;
           launch_cheby_iterate(c->f, c->L, c->g, S.ch_a[1], S.ch_b[1], c->stream);
+          if ((rc = prof_end(c, TL_KERNEL_CHEBY_ITERATE, 1))) return rc;
           if ((rc = S.norm(c->f.r, &old_error))) return rc;
           const double it_alpha = o->eps / 2.0 * std::sqrt(bb / old_error);
           const double gamm = (std::sqrt(c->cn) - 1.0) / (std::sqrt(c->cn) + 1.0);
           est_itc = (int)std::lround(std::log(it_alpha) / std::log(gamm));
           cheby_calc_steps = 1;
         } else {
+          if ((rc = prof_begin(c))) return rc;
           launch_cheby_iterate(c->f, c->L, c->g, S.ch_a[cheby_calc_steps], S.ch_b[cheby_calc_steps], c->stream);
+          if ((rc = prof_end(c, TL_KERNEL_CHEBY_ITERATE, 1))) return rc;
           if (n >= est_itc && n % 10 == 0) {
             if ((rc = S.norm(c->f.r, &error))) return rc;
           }
@@ -1200,7 +1250,9 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
       }
       cheby_calc_steps += 1;
     } else if (S.use_jacobi) {
+      if ((rc = prof_begin(c))) return rc;
       launch_jacobi(c->f, c->L, c->rd(), c->stream);
+      if ((rc = prof_end(c, TL_KERNEL_JACOBI, 1))) return rc;
       if ((rc = check_launch("jacobi"))) return rc;
       if ((rc = reduce_result(c, &error))) return rc;
     }

@@ -103,7 +103,9 @@ void launch_mix_flush_d(const MixFields& m, const Layout& L, MixState* ms, cudaS
 // mirror: off-domain neighbours mirrored (CG); else read from the halo cells (Chebyshev)
 void launch_mix_trial(const Fields& f, const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms,
                       bool first, cudaStream_t s, bool mirror = true);
-void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms, cudaStream_t s);
+// one FP32 CG step: k_mix_w then k_mix_ur; `between` (nullable) is recorded between them
+void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms, cudaStream_t s,
+                          cudaEvent_t between = nullptr);
 // accept the correction: u += d (FP64), d = 0
 void launch_mix_apply(const Fields& f, const MixFields& m, const Layout& L, cudaStream_t s);
 

@@ -350,13 +350,15 @@ void launch_mix_flush_d(const MixFields& m, const Layout& L, MixState* ms, cudaS
   { ++launch_counter(); k_mix_flush_d<<<grid, 256, 0, s>>>(m, L, ms); }
 }
 
-void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms, cudaStream_t s) {
+void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms, cudaStream_t s,
+                          cudaEvent_t between) {
   const int ns = mstrips(L);
   int rows = (int)(((long long)L.ny * ns) / (152 * 8));
   rows = rows < 8 ? 8 : (rows > 64 ? 64 : rows);
   const int min_rows = (int)(((long long)L.ny * ns + MAX_REDUCE_BLOCKS - 1) / MAX_REDUCE_BLOCKS);
   if (rows < min_rows) rows = min_rows;
   { ++launch_counter(); k_mix_w<<<dim3(ns, (L.ny + rows - 1) / rows), MT, 0, s>>>(m, L, rd, ms, rows); }
+  if (between) cudaEventRecord(between, s);
   int gy = L.ny < 512 ? L.ny : 512;
   if ((long long)gy * ns > MAX_REDUCE_BLOCKS) gy = MAX_REDUCE_BLOCKS / ns;
   { ++launch_counter(); k_mix_ur<<<dim3(ns, gy), MT, 0, s>>>(m, L, rd, ms); }

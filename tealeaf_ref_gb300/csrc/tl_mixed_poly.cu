@@ -42,15 +42,16 @@ __device__ __forceinline__ float apply_a32(const float* __restrict__ v, const Mi
 }
 
 // tea_leaf_kernel_ppcg_init_sd (tea_leaf_ppcg_kernel.f90:31-88, no preconditioner) in FP32:
-// rtemp = r, sd = r / theta, utemp = sd.
-__global__ void k_poly_ppcg_init(const double* __restrict__ r, MixFields m, Layout L, double theta) {
+// rtemp = r, sd = r / theta (as r * (1/theta) in FP32: a per-cell FP64 division would make this
+// copy FP64-bound), utemp = sd.
+__global__ void k_poly_ppcg_init(const double* __restrict__ r, MixFields m, Layout L, float inv_theta) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (j > L.nx) return;
   for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
     const long long c = L.at(j, k);
-    const double rv = r[c];
-    const float sd = (float)(rv / theta);
-    m.r[c] = (float)rv;
+    const float rv = (float)r[c];
+    const float sd = rv * inv_theta;
+    m.r[c] = rv;
     m.p[c] = sd;
     m.w[c] = sd;
   }
@@ -129,7 +130,7 @@ __global__ void k_poly_clear(MixFields m, Layout L) {
 void launch_poly_ppcg_inner(const Fields& f, const MixFields& m, const Layout& L, double theta, int inner_steps,
                             const double* ch_a, const double* ch_b, cudaStream_t s) {
   const dim3 g = poly_grid(L);
-  { ++launch_counter(); k_poly_ppcg_init<<<g, PT, 0, s>>>(f.r, m, L, theta); }
+  { ++launch_counter(); k_poly_ppcg_init<<<g, PT, 0, s>>>(f.r, m, L, (float)(1.0 / theta)); }
   if (inner_steps <= 0) {
     { ++launch_counter(); k_poly_to_z<<<g, PT, 0, s>>>(m, L, f.z); }
     return;

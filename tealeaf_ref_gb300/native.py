@@ -110,7 +110,8 @@ SIGNATURES = {
     "tl_profile_read": (_I, [_P, _I, _DP, C.POINTER(C.c_longlong)]),
 }
 
-KERNEL_TIMERS = {"cg_matvec": 0, "cg_update": 1}
+KERNEL_TIMERS = {"cg_matvec": 0, "cg_update": 1, "cheby_iterate": 2, "ppcg_inner": 3, "jacobi": 4,
+                 "mix_matvec": 5, "mix_update": 6, "poly_step": 7}
 
 
 def library_path() -> str:

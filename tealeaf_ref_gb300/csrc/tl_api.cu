@@ -1160,7 +1160,46 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
       continue;
     }
 
-    // ---- Chebyshev / PPCG / Jacobi iteration n (host-driven over the per-kernel path) ----
+    if (S.use_jacobi) {
+      // device-resident Jacobi loop: un and u swap between the u and r fields; iteration m
+      // reads (m odd ? u : r) and writes the other
+      LoopArgs la = c->loop();
+      while (H.status == RUN) {
+        const int n_before = H.n;
+        for (int i = 0; i < batch; ++i) {
+          const int m = n_before + i;
+          const double* un = (m & 1) ? c->f.u : c->f.r;
+          double* uo = (m & 1) ? c->f.r : c->f.u;
+          if (c->prof) CK(cudaEventRecord(c->pev[2 * i], c->stream));
+          launch_fused_jacobi(la, un, uo, c->stream);
+          if (c->prof) CK(cudaEventRecord(c->pev[2 * i + 1], c->stream));
+        }
+        if ((rc = check_launch("jacobi batch"))) return rc;
+        if ((rc = sync_state(c))) return rc;
+        if (c->prof) {
+          int ran = (H.status == EXIT_CONVERGED || H.status == EXIT_BREAKDOWN) ? H.n_exit - n_before + 1
+                                                                                 : H.n - n_before;
+          ran = std::min(std::max(ran, 0), batch);
+          for (int i = 0; i < ran; ++i) {
+            float a = 0.f;
+            CK(cudaEventElapsedTime(&a, c->pev[2 * i], c->pev[2 * i + 1]));
+            c->prof_ms[TL_KERNEL_JACOBI] += a;
+          }
+          c->prof_n[TL_KERNEL_JACOBI] += ran;
+        }
+      }
+      if (H.status == EXIT_BREAKDOWN) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite Jacobi error");
+      // the last iteration computed: n_exit when converged, max_iters otherwise
+      const int last = H.status == EXIT_CONVERGED ? H.n_exit : H.n - 1;
+      if (last >= 1 && (last & 1)) launch_copy_interior(c->f.u, c->f.r, c->L, c->stream);
+      if ((rc = do_halo(c, M(TL_FIELD_U), 1))) return rc;
+      error = H.error;
+      n = H.status == EXIT_CONVERGED ? H.n_exit : H.n;
+      exited = H.status == EXIT_CONVERGED;
+      break;
+    }
+
+    // ---- Chebyshev / PPCG iteration n (host-driven over the per-kernel path) ----
     if ((S.use_cheby || S.use_ppcg) && ch_switch_check) {
       if (cheby_calc_steps == 0) {
         max_cheby_iters = max_iters - n + 2;
@@ -1249,12 +1288,6 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
         rro = rrn;
       }
       cheby_calc_steps += 1;
-    } else if (S.use_jacobi) {
-      if ((rc = prof_begin(c))) return rc;
-      launch_jacobi(c->f, c->L, c->rd(), c->stream);
-      if ((rc = prof_end(c, TL_KERNEL_JACOBI, 1))) return rc;
-      if ((rc = check_launch("jacobi"))) return rc;
-      if ((rc = reduce_result(c, &error))) return rc;
     }
     if ((rc = do_halo(c, fields_mask, 1))) return rc;
     error = std::sqrt(std::fabs(error));

@@ -388,6 +388,43 @@ void launch_fused_cg_ur(const LoopArgs& a, bool ppcg, cudaStream_t s) {
   }
 }
 
+namespace {
+
+struct EpiJacobi {
+  LoopState* st;
+  __device__ void operator()(double (&acc)[1]) const { finish_iteration(st, acc[0]); }
+};
+
+// Jacobi iteration n (tea_leaf_jacobi_solve_kernel, jacobi_kernel.f90:26-77) with un and u in
+// two buffers swapped every iteration instead of the copy un = u: u_out = (u0 + rx(Kx(j+1)
+// un(j+1) + Kx(j) un(j-1)) + ry(Ky(k+1) un(k+1) + Ky(k) un(k-1))) / denominator, error =
+// sum |u_out - un|; the epilogue applies the loop's test (error = sqrt|error|) and n = n+1.
+// Off-domain neighbours of un are zero: the reference never writes un's halo.  The same
+// operation order as k_jacobi, so the same bits.
+__global__ void k_fused_jacobi(Fields f, Layout L, Reduce rd, const double* __restrict__ un, double* __restrict__ u_out) {
+  if (rd.st->status != RUN) return;
+  double v[1] = {0.0};
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
+    if (j > L.nx) continue;
+    const long long c = L.at(j, k);
+    const double ur = j < L.nx ? un[c + 1] : 0.0, ul = j > 1 ? un[c - 1] : 0.0;
+    const double ut = k < L.ny ? un[c + L.ld] : 0.0, ub = k > 1 ? un[c - L.ld] : 0.0;
+    const double num = (f.u0[c] + (f.cx[c + 1] * ur + f.cx[c] * ul)) + (f.cy[c + L.ld] * ut + f.cy[c] * ub);
+    const double u = num * f.jinv[c];
+    u_out[c] = u;
+    v[0] += fabs(u - un[c]);
+  }
+  grid_reduce<1>(v, rd, EpiJacobi{rd.st});
+}
+
+}  // namespace
+
+void launch_fused_jacobi(const LoopArgs& a, const double* un, double* u_out, cudaStream_t s) {
+  const int gy = a.L.ny < 256 ? a.L.ny : 256;
+  { ++launch_counter(); k_fused_jacobi<<<dim3((a.L.nx + 255) / 256, gy), 256, 0, s>>>(a.f, a.L, a.rd, un, u_out); }
+}
+
 void launch_flush_u(const LoopArgs& a, cudaStream_t s) {
   dim3 grid((a.L.nx + FT - 1) / FT, a.L.ny < 4096 ? a.L.ny : 4096);
   { ++launch_counter(); k_flush_u<<<grid, FT, 0, s>>>(a); }

@@ -75,9 +75,8 @@ void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s);
 void launch_fused_cg_ur(const LoopArgs& a, bool ppcg, cudaStream_t s);
 // u += alpha p of the last CG iteration when it is still pending (end of a CG phase)
 void launch_flush_u(const LoopArgs& a, cudaStream_t s);
-void launch_fused_cheby(const LoopArgs& a, const double* u_in, double* u_out, cudaStream_t s);
-void launch_fused_ppcg_inner(const LoopArgs& a, const double* sd_in, double* sd_out, int step, bool last,
-                             cudaStream_t s);
+// one Jacobi iteration from un into u_out (the two swap every iteration), error and the loop's
+// test in the epilogue
 void launch_fused_jacobi(const LoopArgs& a, const double* un, double* u_out, cudaStream_t s);
 void launch_jacobi_denominator(const Fields& f, const Layout& L, const Geometry& g, cudaStream_t s);
 

@@ -58,6 +58,8 @@ SOLVE_CASES = [
     dict(solver="ppcg", ppcg_inner_steps=6, ch_cg_presteps=15, precond="jac_block"),
     dict(solver="ppcg", ppcg_inner_steps=8, ch_cg_presteps=20, reflective=True),
     dict(solver="jacobi", max_iters=300, eps=1e-10),
+    dict(solver="jacobi", max_iters=301, eps=1e-10, reflective=True),
+    dict(solver="jacobi", max_iters=20000, eps=1e-5, nx=24, ny=17, n_rect=2, n_circ=0),
 ]
 
 

@@ -72,6 +72,9 @@ def parse():
                          "4096^2 workloads (Jacobi: 8 rectangles, seed 2, capped at --iters; Chebyshev / PPCG: "
                          "seed 3, 20 CG presteps, PPCG 10 inner steps, solved to tl_eps) and report per-kernel "
                          "GB/s from a separately profiled step")
+    ap.add_argument("--ch-cg-epslim", type=float, default=None,
+                    help="chebyshev / ppcg: override tl_ch_cg_epslim (the error below which CG hands over "
+                         "after its presteps; a large value switches right after them)")
     return ap.parse_args()
 
 
@@ -350,6 +353,8 @@ def run_solver(args):
     else:
         d = dk.config_deck(3, solver=args.solver, cells=cells_n)
         d.ch_cg_presteps = 20
+        if args.ch_cg_epslim is not None:
+            d.ch_cg_epslim = args.ch_cg_epslim
     opts = native.opts_from_deck(d, args.precision)
     dt = d.initial_timestep
     cells = cells_n * cells_n

@@ -736,11 +736,12 @@ namespace {
 int ensure_mix(tl_ctx* c) {
   if (c->mix_slab) return TL_OK;
   const size_t fb = ((size_t)c->L.elems() * sizeof(float) + 4 * 256 + 255) / 256 * 256;
-  CK(cudaMalloc(&c->mix_slab, fb * 8));
-  CK(cudaMemsetAsync(c->mix_slab, 0, fb * 8, c->stream));
+  CK(cudaMalloc(&c->mix_slab, fb * 9));
+  CK(cudaMemsetAsync(c->mix_slab, 0, fb * 9, c->stream));
   float* b = reinterpret_cast<float*>(c->mix_slab);
   const size_t step = fb / sizeof(float);
-  c->mix = MixFields{b, b + step, b + 2 * step, b + 3 * step, b + 4 * step, b + 5 * step, b + 6 * step, b + 7 * step};
+  c->mix = MixFields{b,            b + step,     b + 2 * step, b + 3 * step, b + 4 * step,
+                     b + 5 * step, b + 6 * step, b + 7 * step, b + 8 * step};
   CK(cudaMalloc(&c->mst, sizeof(MixState)));
   CK(cudaMallocHost(&c->mst_host, sizeof(MixState)));
   return TL_OK;

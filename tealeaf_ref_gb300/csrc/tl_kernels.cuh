@@ -84,6 +84,7 @@ void launch_jacobi_denominator(const Fields& f, const Layout& L, const Geometry&
 struct MixFields {
   float *cx, *cy, *di;  // FP32 copies of the pre-scaled operator
   float *r, *p, *p2, *w, *d;
+  float* e;             // second buffer of the blocked polynomial sweeps' ping-pong
 };
 struct MixState {
   double rro, rro_prev, pw, rr, alpha, beta;  // FP32-vector CG scalars (FP64)

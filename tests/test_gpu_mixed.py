@@ -145,3 +145,26 @@ def test_mixed_rejected_for_jacobi_and_preconditioners():
             with pytest.raises(native.TeaLeafError) as e:
                 c.tea_leaf(native.opts_from_deck(d, precision="mixed"), d.initial_timestep)
             assert e.value.code == -1
+
+
+@pytest.mark.parametrize("solver", ["ppcg", "chebyshev"])
+@pytest.mark.parametrize("reflective", [False, True])
+def test_blocked_poly_sweeps_bitwise(solver, reflective, monkeypatch):
+    """The temporally blocked FP32 sweeps (several polynomial steps per pass over the mesh)
+    give the bits of the one-step sweeps: same solution and iteration counts for 1, 3 and 4
+    steps per sweep, on a mesh whose width and height cut the warp strips and row ranges
+    raggedly."""
+    from tealeaf_ref_gb300 import native
+
+    d = small_deck(nx=301, ny=133, steps=2, n_rect=4, n_circ=2, solver=solver, ppcg_inner_steps=10,
+                   ch_cg_presteps=20, reflective=reflective, max_iters=20000)
+    opts = native.opts_from_deck(d, precision="mixed")
+    runs = []
+    for per_sweep in ("1", "4", "3"):
+        monkeypatch.setenv("TL_POLY_STEPS_PER_SWEEP", per_sweep)
+        with native.Chunk.from_deck(d) as c:
+            its = [c.tea_leaf(opts, d.initial_timestep).reported_iterations for _ in range(d.end_step)]
+            runs.append((c.download("u"), its))
+    for u, its in runs[1:]:
+        assert its == runs[0][1]
+        np.testing.assert_array_equal(u, runs[0][0])

@@ -133,8 +133,10 @@ __global__ void k_poly_clear(MixFields m, Layout L) {
 // m, level 0 loads row m and level t = 1..S computes step t at row m - t from level t-1's rows
 // m-t-1 .. m-t+1 (a three-row register window per level) and level t-1's cell values of row m-t
 // (its output one march position earlier).  Horizontal neighbours come from the adjacent
-// lanes by shuffles; the coefficient rows sit in a per-warp shared-memory ring, loaded once
-// at level 0.  Warps never wait for one another.  Level t is exact on local columns
+// lanes by shuffles.  Level 0's rows (coefficients and input state) are staged TB_P rows ahead
+// into per-warp shared-memory rings by asynchronous copies (cp.async), so a march step does not
+// wait for a load; every level reads the coefficients from the ring.  Warps never wait for one
+// another.  Level t is exact on local columns
 // [t, 128-t): with S <= TB_HX the output columns are exact.  Every cell runs the one-step
 // kernels' arithmetic in the same order, so S steps here give the bits of S one-step sweeps.
 // Traffic per S steps: the state and the coefficients read once (x 128/TB_W for the halo),
@@ -143,6 +145,7 @@ constexpr int TB_S = 4;                // steps per sweep at most
 constexpr int TB_HX = 4;               // halo columns on each side of a warp strip
 constexpr int TB_W = 128 - 2 * TB_HX;  // output columns per warp strip
 constexpr int TB_WARPS = 4;            // warps per CTA
+constexpr int TB_P = 2;                // rows staged ahead by asynchronous copies
 constexpr int TB_PF = 8;               // L2 prefetch distance in rows
 constexpr unsigned FULL = 0xffffffffu;
 
@@ -167,18 +170,6 @@ struct PolyArgs {
 
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
-// columns j .. j+3 (j = 1 mod 4, so 16-byte aligned) where lo <= column <= hi, else 0
-__device__ __forceinline__ void load4(const float* __restrict__ p, long long c, int j, int lo, int hi,
-                                      float (&v)[4]) {
-  if (j >= lo && j + 3 <= hi) {
-    const float4 q = __ldg(reinterpret_cast<const float4*>(p + c));
-    v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
-  } else {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) v[i] = (j + i >= lo && j + i <= hi) ? __ldg(p + c + i) : 0.f;
-  }
-}
-
 // columns j+i with lo <= j+i <= hi
 __device__ __forceinline__ void store4(float* __restrict__ p, long long c, const float (&v)[4], int lo, int hi,
                                        int j) {
@@ -191,9 +182,50 @@ __device__ __forceinline__ void store4(float* __restrict__ p, long long c, const
   }
 }
 
+// Per-warp shared memory of the blocked sweep: a ring of RING coefficient rows (di, cx, cy, and
+// Chebyshev's right-hand side; 132 floats per array row) and a ring of TB_P+1 input-state rows.
+template <int MODE, int S>
+struct TbSmem {
+  static constexpr int NC = MODE == POLY_PPCG ? 3 : 4;
+  static constexpr int RING = S + 1 + TB_P;
+  static constexpr int SSLOT = (MODE == POLY_PPCG ? 3 : 2) * 128;  // floats (PPCG: or 128 doubles)
+  static constexpr int WARP_FLOATS = RING * NC * 132 + (TB_P + 1) * SSLOT;
+  static constexpr int BYTES = TB_WARPS * WARP_FLOATS * 4;
+};
+
+__device__ __forceinline__ void cp_async16(float* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N)); }
+
+// columns j .. j+3 of a float row into shared memory: an asynchronous 16-byte copy when all four
+// lie in [lo, hi], else guarded loads (zero outside)
+__device__ __forceinline__ void stage4(float* dst, const float* __restrict__ src, int j, int lo, int hi) {
+  if (j >= lo && j + 3 <= hi) {
+    cp_async16(dst, src);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) dst[i] = (j + i >= lo && j + i <= hi) ? __ldg(src + i) : 0.f;
+  }
+}
+__device__ __forceinline__ void stage4d(double* dst, const double* __restrict__ src, int j, int lo, int hi) {
+  if (j >= lo && j + 3 <= hi) {
+    cp_async16(reinterpret_cast<float*>(dst), src);
+    cp_async16(reinterpret_cast<float*>(dst + 2), src + 2);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) dst[i] = (j + i >= lo && j + i <= hi) ? __ldg(src + i) : 0.0;
+  }
+}
+
 template <int MODE, int S>
 __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
   constexpr bool PPCG = MODE == POLY_PPCG;
+  using SM = TbSmem<MODE, S>;
+  constexpr int NC = SM::NC, RING = SM::RING;
   const int lane = threadIdx.x & 31;
   const int task = blockIdx.x * TB_WARPS + (threadIdx.x >> 5);
   if (task >= a.ntasks) return;  // whole warps only
@@ -204,6 +236,36 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
   const int k1 = min(k0 + a.rows - 1, L.ny);
   const int j = x0 - TB_HX + 4 * lane;  // this lane's first column
   const int out0 = x0, out1 = min(x0 + TB_W - 1, L.nx);
+  const int lc = 4 * lane;
+  extern __shared__ __align__(16) float tb_smem[];
+  float* const wbase = tb_smem + (threadIdx.x >> 5) * SM::WARP_FLOATS;
+  auto coef = [&](int row, int arr) { return wbase + ((row % RING) * NC + arr) * 132; };
+  auto state = [&](int row, int arr) { return wbase + RING * NC * 132 + (row % (TB_P + 1)) * SM::SSLOT + arr * 128; };
+  const int crow_max = min(L.ny + 1, k1 + S);  // coefficient rows (cy also of the boundary row ny+1)
+  const int srow_max = min(L.ny, k1 + S);      // input-state rows
+  // stage row `row` (coefficients and input state) into the rings; one commit group per row
+  auto issue_row = [&](int row) {
+    if (row <= crow_max) {
+      const long long c = L.at(j, row);
+      stage4(coef(row, 2) + lc, m.cy + c, j, 1, L.nx);
+      if (row <= L.ny) {
+        stage4(coef(row, 0) + lc, m.di + c, j, 1, L.nx);
+        stage4(coef(row, 1) + lc, m.cx + c, j, 1, L.nx + 1);
+        if (!PPCG) stage4(coef(row, 3) + lc, m.r + c, j, 1, L.nx);
+      }
+    }
+    if (row <= srow_max) {
+      const long long c = L.at(j, row);
+      if (a.first) {
+        if (PPCG) stage4d(reinterpret_cast<double*>(state(row, 0)) + lc, a.r64 + c, j, 1, L.nx);
+      } else {
+        stage4(state(row, 0) + lc, a.x_in + c, j, 1, L.nx);
+        stage4(state(row, 1) + lc, a.c1_in + c, j, 1, L.nx);
+        if (PPCG) stage4(state(row, 2) + lc, a.c2_in + c, j, 1, L.nx);
+      }
+    }
+    cp_async_commit();
+  };
   float X[S][3][4];   // level t < S: stencil variable of rows (newest-2, newest-1, newest)
   float C1[S][2][4];  // level t < S: rtemp | p of rows (newest-1, newest)
   float C2[S][2][4];  // level t < S: utemp of rows (newest-1, newest)
@@ -214,75 +276,57 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
       X[t][0][i] = X[t][1][i] = X[t][2][i] = 0.f;
       C1[t][0][i] = C1[t][1][i] = C2[t][0][i] = C2[t][1][i] = 0.f;
     }
-  // per-warp ring of coefficient rows (di, cx, cy, and Chebyshev's right-hand side): row q in
-  // slot q mod (S+1), loaded once at level 0 and read by every level from shared memory
-  constexpr int NC = PPCG ? 3 : 4;
-  constexpr int RING = S + 1;
-  __shared__ __align__(16) float ring[TB_WARPS][RING][NC][132];
-  float(*cr)[NC][132] = ring[threadIdx.x >> 5];
-  const int lc = 4 * lane;
   const int mstart = max(1, k0 - S), mend = k1 + S;
+#pragma unroll
+  for (int r = 0; r < TB_P; ++r) issue_row(mstart + r);
   for (int mm = mstart; mm <= mend; ++mm) {
-    // L2 prefetch of the rows the march reaches TB_PF positions later
-    const int pf = mm + TB_PF;
-    if (pf <= min(L.ny, k1 + S) && j >= 1 && j + 3 <= L.nx) {
+    __syncwarp();  // every lane is done with the slots the next copies overwrite
+    issue_row(mm + TB_P);
+    const int pf = mm + TB_PF;  // L2 prefetch further ahead
+    if (pf <= srow_max && j >= 1 && j + 3 <= L.nx) {
       const long long c = L.at(j, pf);
-      if (a.first) {
-        if (PPCG) prefetch_l2(a.r64 + c);
-      } else {
+      if (!a.first) {
         prefetch_l2(a.x_in + c);
         prefetch_l2(a.c1_in + c);
         if (PPCG) prefetch_l2(a.c2_in + c);
+      } else if (PPCG) {
+        prefetch_l2(a.r64 + c);
       }
       prefetch_l2(m.di + c);
       prefetch_l2(m.cx + c);
       prefetch_l2(m.cy + c);
       if (!PPCG) prefetch_l2(m.r + c);
     }
-    // ---- level 0: coefficient row mm into the ring (cy also for the boundary row ny+1) ----
-    __syncwarp();  // every lane is done with the slot's previous row
-    if (mm <= min(L.ny + 1, k1 + S)) {
-      const long long c = L.at(j, mm);
-      float(*slot)[132] = cr[mm % RING];
-      float v0[4], v1[4], v2[4], v3[4];
-      load4(m.cy, c, j, 1, L.nx, v2);
-      if (mm <= L.ny) {
-        load4(m.di, c, j, 1, L.nx, v0);
-        load4(m.cx, c, j, 1, L.nx + 1, v1);
-        if (!PPCG) load4(m.r, c, j, 1, L.nx, v3);
-        *reinterpret_cast<float4*>(&slot[0][lc]) = make_float4(v0[0], v0[1], v0[2], v0[3]);
-        *reinterpret_cast<float4*>(&slot[1][lc]) = make_float4(v1[0], v1[1], v1[2], v1[3]);
-        if (!PPCG) *reinterpret_cast<float4*>(&slot[NC - 1][lc]) = make_float4(v3[0], v3[1], v3[2], v3[3]);
-      }
-      *reinterpret_cast<float4*>(&slot[2][lc]) = make_float4(v2[0], v2[1], v2[2], v2[3]);
-    }
+    cp_async_wait<TB_P>();  // row mm has landed
+    __syncwarp();
     // ---- level 0: the sweep's input at row mm ----
     float nx[4] = {0.f, 0.f, 0.f, 0.f}, n1[4] = {0.f, 0.f, 0.f, 0.f}, n2[4] = {0.f, 0.f, 0.f, 0.f};
-    if (mm <= min(L.ny, k1 + S)) {
-      const long long c = L.at(j, mm);
+    if (mm <= srow_max) {
       if (a.first) {
         if (PPCG) {
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-            if (j + i >= 1 && j + i <= L.nx) {
-              const float rv = (float)a.r64[c + i];
-              n1[i] = rv;
-              nx[i] = rv * a.inv_theta;
-              n2[i] = nx[i];
-            }
-        } else {
-          float rr[4];
-          load4(m.r, c, j, 1, L.nx, rr);
+          const double* rs = reinterpret_cast<const double*>(state(mm, 0)) + lc;
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
-            nx[i] = rr[i] * a.inv_theta;
+            const float rv = (float)rs[i];
+            n1[i] = rv;
+            nx[i] = rv * a.inv_theta;
+            n2[i] = nx[i];
+          }
+        } else {
+          const float* rs = coef(mm, 3) + lc;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            nx[i] = rs[i] * a.inv_theta;
             n1[i] = nx[i];
           }
         }
       } else {
-        load4(a.x_in, c, j, 1, L.nx, nx);
-        load4(a.c1_in, c, j, 1, L.nx, n1);
-        if (PPCG) load4(a.c2_in, c, j, 1, L.nx, n2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          nx[i] = state(mm, 0)[lc + i];
+          n1[i] = state(mm, 1)[lc + i];
+          if (PPCG) n2[i] = state(mm, 2)[lc + i];
+        }
       }
     }
 #pragma unroll
@@ -295,7 +339,6 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
       C2[0][0][i] = C2[0][1][i];
       C2[0][1][i] = n2[i];
     }
-    __syncwarp();  // the ring row is visible to the whole warp
     // ---- levels 1..S: step t at row mm - t ----
 #pragma unroll
     for (int t = 1; t <= S; ++t) {
@@ -303,18 +346,20 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
       const bool act = q >= max(1, k0 - (S - t)) && q <= min(L.ny, k1 + (S - t));  // uniform per warp
       float ox[4] = {0.f, 0.f, 0.f, 0.f}, o1[4] = {0.f, 0.f, 0.f, 0.f}, o2[4] = {0.f, 0.f, 0.f, 0.f};
       if (act) {
-        const float(*rq)[132] = cr[q % RING];
-        const float(*rq1)[132] = cr[(q + 1) % RING];
+        const float* rdi = coef(q, 0) + lc;
+        const float* rcx = coef(q, 1) + lc;
+        const float* rcy = coef(q, 2) + lc;
+        const float* rcy1 = coef(q + 1, 2) + lc;
         float di[4], cxv[4], cyb[4], cyt[4], rhs[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          di[i] = rq[0][lc + i];
-          cxv[i] = rq[1][lc + i];
-          cyb[i] = rq[2][lc + i];
-          cyt[i] = rq1[2][lc + i];
-          rhs[i] = PPCG ? 0.f : rq[NC - 1][lc + i];
+          di[i] = rdi[i];
+          cxv[i] = rcx[i];
+          cyb[i] = rcy[i];
+          cyt[i] = rcy1[i];
+          rhs[i] = PPCG ? 0.f : coef(q, NC - 1)[lc + i];
         }
-        const float cx4 = rq[1][lc + 4];                                // cx at column j+4
+        const float cx4 = rcx[4];                                       // cx at column j+4
         const float left = __shfl_up_sync(FULL, X[t - 1][1][3], 1);     // column j-1
         const float right = __shfl_down_sync(FULL, X[t - 1][1][0], 1);  // column j+4
 #pragma unroll
@@ -372,6 +417,7 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
       }
     }
   }
+  cp_async_wait<0>();  // no copy outstanding when the warp exits
 }
 
 // Steps per blocked sweep: TB_S, or TL_POLY_STEPS_PER_SWEEP (1 .. TB_S) from the environment;
@@ -393,16 +439,23 @@ void tb_tasks(PolyArgs& a, const Layout& L) {
   a.ntasks = a.nstrips * ((L.ny + rows - 1) / rows);
 }
 
+template <int MODE, int S>
+void launch_tb_s(const PolyArgs& a, dim3 grid, cudaStream_t s) {
+  constexpr int bytes = TbSmem<MODE, S>::BYTES;
+  // above the 48 KB default: the attribute is set on the current device before each launch
+  cudaFuncSetAttribute(k_poly_tb<MODE, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  k_poly_tb<MODE, S><<<grid, 32 * TB_WARPS, bytes, s>>>(a);
+}
+
 template <int MODE>
 void launch_tb(const PolyArgs& a, int steps, cudaStream_t s) {
   const dim3 grid((a.ntasks + TB_WARPS - 1) / TB_WARPS);
-  const int nt = 32 * TB_WARPS;
   ++launch_counter();
   switch (steps) {
-    case 1: k_poly_tb<MODE, 1><<<grid, nt, 0, s>>>(a); break;
-    case 2: k_poly_tb<MODE, 2><<<grid, nt, 0, s>>>(a); break;
-    case 3: k_poly_tb<MODE, 3><<<grid, nt, 0, s>>>(a); break;
-    default: k_poly_tb<MODE, 4><<<grid, nt, 0, s>>>(a); break;
+    case 1: launch_tb_s<MODE, 1>(a, grid, s); break;
+    case 2: launch_tb_s<MODE, 2>(a, grid, s); break;
+    case 3: launch_tb_s<MODE, 3>(a, grid, s); break;
+    default: launch_tb_s<MODE, 4>(a, grid, s); break;
   }
 }
 

@@ -239,29 +239,32 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
   const int lc = 4 * lane;
   extern __shared__ __align__(16) float tb_smem[];
   float* const wbase = tb_smem + (threadIdx.x >> 5) * SM::WARP_FLOATS;
-  auto coef = [&](int row, int arr) { return wbase + ((row % RING) * NC + arr) * 132; };
-  auto state = [&](int row, int arr) { return wbase + RING * NC * 132 + (row % (TB_P + 1)) * SM::SSLOT + arr * 128; };
+  // ring slots: row r sits in coefficient slot (r - mstart) mod RING and state slot
+  // (r - mstart) mod (TB_P+1); the march keeps the slots of row mm in running counters
+  auto coef = [&](int slot, int arr) { return wbase + (slot * NC + arr) * 132; };
+  auto state = [&](int slot, int arr) { return wbase + RING * NC * 132 + slot * SM::SSLOT + arr * 128; };
+  constexpr int SR = TB_P + 1;
   const int crow_max = min(L.ny + 1, k1 + S);  // coefficient rows (cy also of the boundary row ny+1)
   const int srow_max = min(L.ny, k1 + S);      // input-state rows
   // stage row `row` (coefficients and input state) into the rings; one commit group per row
-  auto issue_row = [&](int row) {
+  auto issue_row = [&](int row, int cs, int ss) {
     if (row <= crow_max) {
       const long long c = L.at(j, row);
-      stage4(coef(row, 2) + lc, m.cy + c, j, 1, L.nx);
+      stage4(coef(cs, 2) + lc, m.cy + c, j, 1, L.nx);
       if (row <= L.ny) {
-        stage4(coef(row, 0) + lc, m.di + c, j, 1, L.nx);
-        stage4(coef(row, 1) + lc, m.cx + c, j, 1, L.nx + 1);
-        if (!PPCG) stage4(coef(row, 3) + lc, m.r + c, j, 1, L.nx);
+        stage4(coef(cs, 0) + lc, m.di + c, j, 1, L.nx);
+        stage4(coef(cs, 1) + lc, m.cx + c, j, 1, L.nx + 1);
+        if (!PPCG) stage4(coef(cs, 3) + lc, m.r + c, j, 1, L.nx);
       }
     }
     if (row <= srow_max) {
       const long long c = L.at(j, row);
       if (a.first) {
-        if (PPCG) stage4d(reinterpret_cast<double*>(state(row, 0)) + lc, a.r64 + c, j, 1, L.nx);
+        if (PPCG) stage4d(reinterpret_cast<double*>(state(ss, 0)) + lc, a.r64 + c, j, 1, L.nx);
       } else {
-        stage4(state(row, 0) + lc, a.x_in + c, j, 1, L.nx);
-        stage4(state(row, 1) + lc, a.c1_in + c, j, 1, L.nx);
-        if (PPCG) stage4(state(row, 2) + lc, a.c2_in + c, j, 1, L.nx);
+        stage4(state(ss, 0) + lc, a.x_in + c, j, 1, L.nx);
+        stage4(state(ss, 1) + lc, a.c1_in + c, j, 1, L.nx);
+        if (PPCG) stage4(state(ss, 2) + lc, a.c2_in + c, j, 1, L.nx);
       }
     }
     cp_async_commit();
@@ -278,10 +281,16 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
     }
   const int mstart = max(1, k0 - S), mend = k1 + S;
 #pragma unroll
-  for (int r = 0; r < TB_P; ++r) issue_row(mstart + r);
+  for (int r = 0; r < TB_P; ++r) issue_row(mstart + r, r % RING, r % SR);
+  int cslot = 0, sslot = 0;  // slots of row mm
   for (int mm = mstart; mm <= mend; ++mm) {
     __syncwarp();  // every lane is done with the slots the next copies overwrite
-    issue_row(mm + TB_P);
+    {
+      int cs = cslot + TB_P, ss = sslot + TB_P;
+      if (cs >= RING) cs -= RING;
+      if (ss >= SR) ss -= SR;
+      issue_row(mm + TB_P, cs, ss);
+    }
     const int pf = mm + TB_PF;  // L2 prefetch further ahead
     if (pf <= srow_max && j >= 1 && j + 3 <= L.nx) {
       const long long c = L.at(j, pf);
@@ -304,7 +313,7 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
     if (mm <= srow_max) {
       if (a.first) {
         if (PPCG) {
-          const double* rs = reinterpret_cast<const double*>(state(mm, 0)) + lc;
+          const double* rs = reinterpret_cast<const double*>(state(sslot, 0)) + lc;
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             const float rv = (float)rs[i];
@@ -313,7 +322,7 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
             n2[i] = nx[i];
           }
         } else {
-          const float* rs = coef(mm, 3) + lc;
+          const float* rs = coef(cslot, 3) + lc;
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             nx[i] = rs[i] * a.inv_theta;
@@ -323,9 +332,9 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
       } else {
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          nx[i] = state(mm, 0)[lc + i];
-          n1[i] = state(mm, 1)[lc + i];
-          if (PPCG) n2[i] = state(mm, 2)[lc + i];
+          nx[i] = state(sslot, 0)[lc + i];
+          n1[i] = state(sslot, 1)[lc + i];
+          if (PPCG) n2[i] = state(sslot, 2)[lc + i];
         }
       }
     }
@@ -346,10 +355,13 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
       const bool act = q >= max(1, k0 - (S - t)) && q <= min(L.ny, k1 + (S - t));  // uniform per warp
       float ox[4] = {0.f, 0.f, 0.f, 0.f}, o1[4] = {0.f, 0.f, 0.f, 0.f}, o2[4] = {0.f, 0.f, 0.f, 0.f};
       if (act) {
-        const float* rdi = coef(q, 0) + lc;
-        const float* rcx = coef(q, 1) + lc;
-        const float* rcy = coef(q, 2) + lc;
-        const float* rcy1 = coef(q + 1, 2) + lc;
+        int qs = cslot - t, qs1 = cslot - t + 1;  // slots of rows q and q+1
+        if (qs < 0) qs += RING;
+        if (qs1 < 0) qs1 += RING;
+        const float* rdi = coef(qs, 0) + lc;
+        const float* rcx = coef(qs, 1) + lc;
+        const float* rcy = coef(qs, 2) + lc;
+        const float* rcy1 = coef(qs1, 2) + lc;
         float di[4], cxv[4], cyb[4], cyt[4], rhs[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -357,7 +369,7 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
           cxv[i] = rcx[i];
           cyb[i] = rcy[i];
           cyt[i] = rcy1[i];
-          rhs[i] = PPCG ? 0.f : coef(q, NC - 1)[lc + i];
+          rhs[i] = PPCG ? 0.f : coef(qs, NC - 1)[lc + i];
         }
         const float cx4 = rcx[4];                                       // cx at column j+4
         const float left = __shfl_up_sync(FULL, X[t - 1][1][3], 1);     // column j-1
@@ -416,6 +428,8 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
         }
       }
     }
+    if (++cslot == RING) cslot = 0;
+    if (++sslot == SR) sslot = 0;
   }
   cp_async_wait<0>();  // no copy outstanding when the warp exits
 }

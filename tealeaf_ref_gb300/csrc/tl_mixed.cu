@@ -169,8 +169,31 @@ struct F4 {
   }
 };
 
+// Rows of the FP32 sweep's inputs are staged into a shared-memory ring MP rows ahead by
+// asynchronous copies (cp.async); a staged row holds p_old, r (with the strip's two halo
+// columns), cy, cx (with the strip's right face), Di and d.  Column col of a strip starting at
+// js sits at index col - js + 4, so interior columns are 16-byte aligned.
+constexpr int MP = 2;               // rows staged ahead
+constexpr int MNS = MP + 3;         // ring slots: rows k-1 .. k+1+MP
+constexpr int MRW = MSW + 8;        // floats per staged array row
+constexpr int MARR = 6;             // staged arrays: p_old, r, cy, cx, di, d
+constexpr int MIX_W_SMEM = (MNS * MARR * MRW + 2 * (MSW + 2)) * 4;
+
+__device__ __forceinline__ void mix_cp16(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src));
+}
+__device__ __forceinline__ void mix_cp4(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src));
+}
+__device__ __forceinline__ void mix_commit() { asm volatile("cp.async.commit_group;"); }
+template <int N>
+__device__ __forceinline__ void mix_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N)); }
+
 // p_n = r + beta p_{n-1} (FP32), w = A p_n (FP32), p.w (Dot2), deferred d += alpha p_{n-1}.
-// Same row march as the FP64 sweep (tl_fused.cu), four columns per thread.
+// Same row march as the FP64 sweep (tl_fused.cu), four columns per thread, with the inputs of
+// row k+1+MP staged while row k is computed.
 __global__ void __launch_bounds__(MT) k_mix_w(MixFields m, Layout L, Reduce rd, MixState* ms, int rows_per_cta) {
   if (ms->status != RUN) return;
   const int n = ms->n;
@@ -181,7 +204,8 @@ __global__ void __launch_bounds__(MT) k_mix_w(MixFields m, Layout L, Reduce rd, 
   const float* __restrict__ pold = (n & 1) ? m.p : m.p2;
   float* __restrict__ pout = (n & 1) ? m.p2 : m.p;
   const float* __restrict__ r = m.r;
-  __shared__ float buf[2][MSW + 2];
+  extern __shared__ __align__(16) float mix_smem[];
+  float(*buf)[MSW + 2] = reinterpret_cast<float(*)[MSW + 2]>(mix_smem + MNS * MARR * MRW);
   const int t = threadIdx.x;
   const int js = blockIdx.x * MSW + 1;
   const int ja = js + 4 * t;
@@ -189,51 +213,114 @@ __global__ void __launch_bounds__(MT) k_mix_w(MixFields m, Layout L, Reduce rd, 
   const bool active = nv > 0;
   const int k0 = blockIdx.y * rows_per_cta + 1;
   const int k1 = min(k0 + rows_per_cta - 1, L.ny);
-  auto pnew = [&](long long c, F4& q, F4& old) {
-    old.load(pold, c);
-    q = old;
-    if (upd) {
-      F4 s;
-      s.load(r, c);
-#pragma unroll
-      for (int i = 0; i < 4; ++i) q.v[i] = fmaf(beta, old.v[i], s.v[i]);
+  const int o = 4 * t + 4;  // this thread's first column in a staged row
+  auto arr = [&](int row, int a) { return mix_smem + ((row - k0 + 1) % MNS * MARR + a) * MRW; };
+  enum { A_P = 0, A_R = 1, A_CY = 2, A_CX = 3, A_DI = 4, A_D = 5 };
+  // four columns ja.. of a row of src into dst + o (16-byte copy when all are interior)
+  auto stage4 = [&](float* dst, const float* src, long long c, int hi) {
+    if (ja + 3 <= hi) {
+      mix_cp16(dst + o, src + c);
+    } else {
+      for (int i = 0; i < 4; ++i)
+        if (ja + i <= hi) dst[o + i] = src[c + i];
     }
   };
-  auto pnew1 = [&](long long c) { return upd ? fmaf(beta, pold[c], r[c]) : pold[c]; };
+  // stage row `row` (rows k0-1 .. k1+1; what each array needs of it); one commit group
+  auto stage_row = [&](int row) {
+    if (row >= 1 && row <= L.ny + 1 && row >= k0 - 1 && row <= k1 + 1) {
+      const long long c = L.at(ja, row);
+      if (row <= L.ny) {
+        if (active) {
+          stage4(arr(row, A_P), pold, c, L.nx);
+          if (upd) stage4(arr(row, A_R), r, c, L.nx);
+        }
+        if (t == 0 && js > 1) {  // left halo column js-1
+          const long long ch = L.at(js - 1, row);
+          mix_cp4(arr(row, A_P) + 3, pold + ch);
+          if (upd) mix_cp4(arr(row, A_R) + 3, r + ch);
+        }
+        if (t == MT - 1 && js + MSW <= L.nx) {  // right halo column js+MSW
+          const long long ch = L.at(js + MSW, row);
+          mix_cp4(arr(row, A_P) + MSW + 4, pold + ch);
+          if (upd) mix_cp4(arr(row, A_R) + MSW + 4, r + ch);
+        }
+      }
+      if (row >= k0) {
+        if (active) stage4(arr(row, A_CY), m.cy, c, L.nx);
+        if (row <= k1) {
+          // cx up to the boundary face nx+1: a thread's column ja+4 is staged by the next
+          // thread (also when that one owns no interior column), the strip's last by the last
+          if (ja <= L.nx + 1) stage4(arr(row, A_CX), m.cx, c, L.nx + 1);
+          if (t == MT - 1 && js + MSW <= L.nx + 1) mix_cp4(arr(row, A_CX) + MSW + 4, m.cx + L.at(js + MSW, row));
+          if (active) {
+            stage4(arr(row, A_DI), m.di, c, L.nx);
+            if (upd_d) stage4(arr(row, A_D), m.d, c, L.nx);
+          }
+        }
+      }
+    }
+    mix_commit();
+  };
+  // p_n of four columns of a staged row (old: p_{n-1} there)
+  auto pnew = [&](int row, F4& q, F4& old) {
+    const float* sp = arr(row, A_P) + o;
+    const float* sr = arr(row, A_R) + o;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      old.v[i] = sp[i];
+      q.v[i] = upd ? fmaf(beta, sp[i], sr[i]) : sp[i];
+    }
+  };
+  auto pnew1 = [&](int row, int idx) {
+    const float po = arr(row, A_P)[idx];
+    return upd ? fmaf(beta, po, arr(row, A_R)[idx]) : po;
+  };
+  // prologue: rows k0-1 .. k0+MP
+  for (int rr = k0 - 1; rr <= k0 + MP; ++rr) stage_row(rr);
+  mix_wait<MP>();  // rows k0-1 and k0 have landed
+  __syncthreads();
   Dot2 dot;
   F4 pm{}, pc{}, pnx{}, cyc{}, oc{}, onx{}, junk{};
   if (active) {
-    pnew(L.at(ja, k0), pc, oc);
+    pnew(k0, pc, oc);
     if (k0 == 1)
       pm = pc;
     else
-      pnew(L.at(ja, k0 - 1), pm, junk);
-    cyc.load(m.cy, L.at(ja, k0));
+      pnew(k0 - 1, pm, junk);
+    const float* sc = arr(k0, A_CY) + o;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) cyc.v[i] = sc[i];
   }
   for (int k = k0; k <= k1; ++k) {
     const int b = k & 1;
     const long long c = L.at(ja, k);
-    F4 cyn, cx4, dd, dv, w;
-    float cxr = 0.f;
+    stage_row(k + 1 + MP);
     if (active) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) buf[b][4 * t + 1 + i] = pc.v[i];
+    }
+    if (t == 0 && js > 1) buf[b][0] = pnew1(k, 3);
+    if (t == MT - 1 && js + MSW <= L.nx) buf[b][MSW + 1] = pnew1(k, MSW + 4);
+    mix_wait<MP>();  // row k+1 has landed
+    __syncthreads();
+    if (active) {
+      F4 cyn, cx4, dd, dv, w;
       if (k == L.ny)
         pnx = pc;
       else
-        pnew(L.at(ja, k + 1), pnx, onx);
+        pnew(k + 1, pnx, onx);
+      const float* scy = arr(k + 1, A_CY) + o;
+      const float* scx = arr(k, A_CX) + o;
+      const float* sdi = arr(k, A_DI) + o;
+      const float* sd = arr(k, A_D) + o;
 #pragma unroll
-      for (int i = 0; i < 4; ++i) buf[b][4 * t + 1 + i] = pc.v[i];
-      // this row's coefficient (and correction) loads are issued before the barrier so
-      // that their latency overlaps the wait
-      cyn.load(m.cy, c + L.ld);
-      cx4.load(m.cx, c);
-      dd.load(m.di, c);
-      if (nv == 4) cxr = m.cx[c + 4];
-      if (upd_d) dv.load(m.d, c);
-    }
-    if (t == 0 && js > 1) buf[b][0] = pnew1(L.at(js - 1, k));
-    if (t == MT - 1 && js + MSW <= L.nx) buf[b][MSW + 1] = pnew1(L.at(js + MSW, k));
-    __syncthreads();
-    if (active) {
+      for (int i = 0; i < 4; ++i) {
+        cyn.v[i] = scy[i];
+        cx4.v[i] = scx[i];
+        dd.v[i] = sdi[i];
+        dv.v[i] = upd_d ? sd[i] : 0.f;
+      }
+      const float cxr = (nv == 4) ? scx[4] : 0.f;  // the next thread's first column, or the right face
       const float left0 = (ja == 1) ? pc.v[0] : buf[b][4 * t];
       const float right3 = buf[b][4 * t + 5];
 #pragma unroll
@@ -263,6 +350,7 @@ __global__ void __launch_bounds__(MT) k_mix_w(MixFields m, Layout L, Reduce rd, 
     pc = pnx;
     oc = onx;
   }
+  mix_wait<0>();
   double acc[1] = {dot.value()};
   grid_reduce<1>(acc, rd, EpiMixW{ms});
 }
@@ -357,7 +445,8 @@ void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd,
   rows = rows < 8 ? 8 : (rows > 64 ? 64 : rows);
   const int min_rows = (int)(((long long)L.ny * ns + MAX_REDUCE_BLOCKS - 1) / MAX_REDUCE_BLOCKS);
   if (rows < min_rows) rows = min_rows;
-  { ++launch_counter(); k_mix_w<<<dim3(ns, (L.ny + rows - 1) / rows), MT, 0, s>>>(m, L, rd, ms, rows); }
+  cudaFuncSetAttribute(k_mix_w, cudaFuncAttributeMaxDynamicSharedMemorySize, MIX_W_SMEM);
+  { ++launch_counter(); k_mix_w<<<dim3(ns, (L.ny + rows - 1) / rows), MT, MIX_W_SMEM, s>>>(m, L, rd, ms, rows); }
   if (between) cudaEventRecord(between, s);
   int gy = L.ny < 512 ? L.ny : 512;
   if ((long long)gy * ns > MAX_REDUCE_BLOCKS) gy = MAX_REDUCE_BLOCKS / ns;

@@ -77,6 +77,11 @@ struct tl_ctx {
   bool prof = false;
   cudaEvent_t pev[3 * BATCH] = {};
   cudaEvent_t qe0 = nullptr, qe1 = nullptr;  // one timed launch of a host-driven loop
+  // CUDA graphs of one batch of the device-resident loops (captured once per set of kernel
+  // arguments): the fused CG batch and the mixed-precision CG batch
+  cudaGraphExec_t cg_exec = nullptr, mix_exec = nullptr;
+  LoopArgs cg_key{};
+  long long cg_nk = 0, mix_nk = 0;
   double prof_ms[TL_NUM_KERNEL_TIMERS] = {};
   long long prof_n[TL_NUM_KERNEL_TIMERS] = {};
   long long nlaunch = 0;  // kernels launched by the current tl_tea_leaf call
@@ -190,6 +195,77 @@ int prof_end(tl_ctx* c, int id, int count) {
   CK(cudaEventElapsedTime(&ms, c->qe0, c->qe1));
   c->prof_ms[id] += ms;
   c->prof_n[id] += count;
+  return TL_OK;
+}
+
+// Batches of the device-resident loops as CUDA graphs.  All loop state (iteration index, alpha,
+// beta, status, which p buffer is current) lives in device memory, so one batch of launches
+// has the same arguments every time and is captured once; a launch of the graph replaces
+// 2 x BATCH kernel launches.  Recaptured when an argument changes (dt changes ry; a larger
+// max_iters reallocates the history buffers).
+bool same_loop_args(const LoopArgs& a, const LoopArgs& b) {
+  return memcmp(&a.f, &b.f, sizeof(Fields)) == 0 && a.L.nx == b.L.nx && a.L.ny == b.L.ny && a.L.ld == b.L.ld &&
+         memcmp(&a.rd, &b.rd, sizeof(Reduce)) == 0 && a.precond == b.precond && a.reflective == b.reflective &&
+         a.ry == b.ry;
+}
+
+template <typename F>
+int capture_batch(tl_ctx* c, cudaGraphExec_t* exec, long long* nk, F&& launches) {
+  if (*exec) {
+    cudaGraphExecDestroy(*exec);
+    *exec = nullptr;
+  }
+  const long long before = launch_counter();
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  launches();
+  const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  *nk = launch_counter() - before;
+  launch_counter() = before;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  const cudaError_t ei = cudaGraphInstantiate(exec, g, 0);
+  cudaGraphDestroy(g);
+  if (ei != cudaSuccess) {
+    *exec = nullptr;
+    return cuda_fail(ei, "cudaGraphInstantiate");
+  }
+  return TL_OK;
+}
+
+// TL_NO_GRAPHS=1 in the environment: launch the batches kernel by kernel (same kernels, same
+// results), e.g. under tools that do not follow graph launches.
+bool use_graphs() {
+  const char* e = getenv("TL_NO_GRAPHS");
+  return !(e && e[0] == '1');
+}
+
+int run_cg_batch(tl_ctx* c, const LoopArgs& la) {
+  if (!c->cg_exec || !same_loop_args(c->cg_key, la)) {
+    int rc = capture_batch(c, &c->cg_exec, &c->cg_nk, [&] {
+      for (int i = 0; i < tl_ctx::BATCH; ++i) {
+        launch_fused_cg_w(la, false, c->stream);
+        launch_fused_cg_ur(la, false, c->stream);
+      }
+    });
+    if (rc) return rc;
+    c->cg_key = la;
+  }
+  CK(cudaGraphLaunch(c->cg_exec, c->stream));
+  launch_counter() += c->cg_nk;
+  return TL_OK;
+}
+
+int run_mix_batch(tl_ctx* c, const Reduce& rd) {
+  // the mixed batch's arguments (FP32 fields, layout, reduction buffers, state) are fixed for
+  // a context, except the reduction's history pointers, which the FP32 kernels do not use
+  if (!c->mix_exec) {
+    int rc = capture_batch(c, &c->mix_exec, &c->mix_nk, [&] {
+      for (int i = 0; i < tl_ctx::BATCH; ++i) launch_mix_iteration(c->mix, c->L, rd, c->mst, c->stream);
+    });
+    if (rc) return rc;
+  }
+  CK(cudaGraphLaunch(c->mix_exec, c->stream));
+  launch_counter() += c->mix_nk;
   return TL_OK;
 }
 
@@ -408,6 +484,8 @@ int tl_destroy(tl_ctx* c) {
     if (c->pev[i]) cudaEventDestroy(c->pev[i]);
   if (c->qe0) cudaEventDestroy(c->qe0);
   if (c->qe1) cudaEventDestroy(c->qe1);
+  if (c->cg_exec) cudaGraphExecDestroy(c->cg_exec);
+  if (c->mix_exec) cudaGraphExecDestroy(c->mix_exec);
   cudaFree(c->tape);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -744,6 +822,7 @@ int ensure_mix(tl_ctx* c) {
                      b + 5 * step, b + 6 * step, b + 7 * step, b + 8 * step};
   CK(cudaMalloc(&c->mst, sizeof(MixState)));
   CK(cudaMallocHost(&c->mst_host, sizeof(MixState)));
+  if (prepare_mix_kernels() != 0) return fail(TL_ERR_CUDA, "cannot set the mixed-precision kernels' shared memory");
   return TL_OK;
 }
 
@@ -813,10 +892,14 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
     CK(cudaMemcpyAsync(c->mst, &H, sizeof(MixState), cudaMemcpyHostToDevice, c->stream));
     while (H.status == RUN) {
       const int n_before = H.n;
-      for (int i = 0; i < batch; ++i) {
-        if (c->prof) CK(cudaEventRecord(c->pev[3 * i], c->stream));
-        launch_mix_iteration(c->mix, c->L, rd, c->mst, c->stream, c->prof ? c->pev[3 * i + 1] : nullptr);
-        if (c->prof) CK(cudaEventRecord(c->pev[3 * i + 2], c->stream));
+      if (!c->prof && use_graphs()) {
+        if ((rc = run_mix_batch(c, rd))) return rc;
+      } else {
+        for (int i = 0; i < batch; ++i) {
+          if (c->prof) CK(cudaEventRecord(c->pev[3 * i], c->stream));
+          launch_mix_iteration(c->mix, c->L, rd, c->mst, c->stream, c->prof ? c->pev[3 * i + 1] : nullptr);
+          if (c->prof) CK(cudaEventRecord(c->pev[3 * i + 2], c->stream));
+        }
       }
       if ((rc = check_launch("mixed batch"))) return rc;
       if ((rc = sync_mix(c))) return rc;
@@ -1113,12 +1196,16 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
       // device-resident CG loop, batches of iterations, one status read per batch
       LoopArgs la = c->loop();
       const int n_before = n;
-      for (int i = 0; i < batch; ++i) {
-        if (c->prof) CK(cudaEventRecord(c->pev[3 * i], c->stream));
-        launch_fused_cg_w(la, false, c->stream);
-        if (c->prof) CK(cudaEventRecord(c->pev[3 * i + 1], c->stream));
-        launch_fused_cg_ur(la, false, c->stream);
-        if (c->prof) CK(cudaEventRecord(c->pev[3 * i + 2], c->stream));
+      if (!c->prof && use_graphs()) {
+        if ((rc = run_cg_batch(c, la))) return rc;
+      } else {
+        for (int i = 0; i < batch; ++i) {
+          if (c->prof) CK(cudaEventRecord(c->pev[3 * i], c->stream));
+          launch_fused_cg_w(la, false, c->stream);
+          if (c->prof) CK(cudaEventRecord(c->pev[3 * i + 1], c->stream));
+          launch_fused_cg_ur(la, false, c->stream);
+          if (c->prof) CK(cudaEventRecord(c->pev[3 * i + 2], c->stream));
+        }
       }
       if ((rc = check_launch("cg batch"))) return rc;
       if ((rc = sync_state(c))) return rc;

@@ -96,6 +96,9 @@ struct MixState {
   double d_alpha;
   int n, max_n, phase_end, status, p_pending, d_pending, d_psel;
 };
+// once per context (device), before any launch or capture: the FP32 matvec sweep's dynamic
+// shared memory above the 48 KB default; 0 on success
+int prepare_mix_kernels();
 void launch_mix_prep(const Fields& f, const MixFields& m, const Layout& L, cudaStream_t s);
 // d += alpha p if an update is pending (the host clears MixState::d_pending afterwards)
 void launch_mix_flush_d(const MixFields& m, const Layout& L, MixState* ms, cudaStream_t s);

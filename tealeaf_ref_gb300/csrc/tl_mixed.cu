@@ -438,6 +438,10 @@ void launch_mix_flush_d(const MixFields& m, const Layout& L, MixState* ms, cudaS
   { ++launch_counter(); k_mix_flush_d<<<grid, 256, 0, s>>>(m, L, ms); }
 }
 
+int prepare_mix_kernels() {
+  return cudaFuncSetAttribute(k_mix_w, cudaFuncAttributeMaxDynamicSharedMemorySize, MIX_W_SMEM) == cudaSuccess ? 0 : -1;
+}
+
 void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms, cudaStream_t s,
                           cudaEvent_t between) {
   const int ns = mstrips(L);
@@ -445,7 +449,6 @@ void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd,
   rows = rows < 8 ? 8 : (rows > 64 ? 64 : rows);
   const int min_rows = (int)(((long long)L.ny * ns + MAX_REDUCE_BLOCKS - 1) / MAX_REDUCE_BLOCKS);
   if (rows < min_rows) rows = min_rows;
-  cudaFuncSetAttribute(k_mix_w, cudaFuncAttributeMaxDynamicSharedMemorySize, MIX_W_SMEM);
   { ++launch_counter(); k_mix_w<<<dim3(ns, (L.ny + rows - 1) / rows), MT, MIX_W_SMEM, s>>>(m, L, rd, ms, rows); }
   if (between) cudaEventRecord(between, s);
   int gy = L.ny < 512 ? L.ny : 512;

@@ -388,13 +388,26 @@ class RunResult:
     solves: List[dict]
 
 
-def run_deck(deck: Deck, max_steps: Optional[int] = None, precision: str = "fp64", inner_tol: float = 0.0) -> RunResult:
+def run_deck(deck: Deck, max_steps: Optional[int] = None, precision: str = "fp64", inner_tol: float = 0.0,
+             visit_dir: Optional[str] = None) -> RunResult:
     """The reference's main program on one GPU chunk: start (generate, set_field, first
-    field_summary; start.f90:98-125) then the diffuse loop (diffuse.f90:43-105)."""
+    field_summary; start.f90:98-125) then the diffuse loop (diffuse.f90:43-105).  With
+    ``visit_dir`` and a non-zero visit_frequency, VTK files are written there where the loop
+    calls visit (every visit_frequency steps and at the end; diffuse.f90:58-59,89)."""
     opts = opts_from_deck(deck, precision, inner_tol)
     with Chunk.from_deck(deck) as c:
         summaries = [(0, c.field_summary())]
         solves = []
+        vis = None
+        if visit_dir and deck.visit_frequency:
+            from .visit import Visit
+
+            vis = Visit(visit_dir, deck)
+            density = c.download("density")
+            energy0 = c.download("energy1")  # set_field copied energy0 into energy1
+
+            def visit(step):
+                vis.write(step, density, energy0, c.download("u"))
         step, time = 0, 0.0
         g_small = float(np.float32(1.0e-16))
         while True:
@@ -405,7 +418,11 @@ def run_deck(deck: Deck, max_steps: Optional[int] = None, precision: str = "fp64
             done = time + g_small > deck.end_time or step >= deck.end_step or bool(max_steps and step >= max_steps)
             if deck.summary_frequency and step % deck.summary_frequency == 0 and not done:
                 summaries.append((step, c.field_summary()))
+            if vis and step % deck.visit_frequency == 0:
+                visit(step)
             if done:
                 summaries.append((step, c.field_summary()))
+                if vis:
+                    visit(step)
                 break
         return RunResult(summaries, solves)

@@ -454,16 +454,10 @@ def main():
     if args.solver != "cg":
         run_solver(args)
         return
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch
-        import torch.distributed as dist
+    from tealeaf_ref_gb300 import replicas
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+    grp = replicas.init()
+    world, rank, local = grp.world, grp.rank, grp.local
 
     import numpy as np
 
@@ -479,18 +473,8 @@ def main():
     for _ in range(args.warmup):
         chunk.tea_leaf(opts, dt)
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        import torch
-
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier = grp.barrier
+    max_over_ranks = grp.max
 
     # ---- device-resident timed region ----
     chunk.profile(True)
@@ -509,7 +493,7 @@ def main():
     up_ms, up_n = chunk.profile_read("cg_update")
     chunk.profile(False)
     t_max = max_over_ranks(dev_s)
-    value = world * cells * its / t_max
+    value = replicas.whole_job_rate(world, cells, its, t_max)
 
     # ---- end to end through the C ABI with host buffers ----
     e2e = None
@@ -541,7 +525,7 @@ def main():
             e_wall = time.perf_counter() - t0
         barrier()
         e_wall = max_over_ranks(e_wall)
-        e2e = {"value": world * cells * e_its / e_wall, "unit": "cell-iterations/s",
+        e2e = {"value": replicas.whole_job_rate(world, cells, e_its, e_wall), "unit": "cell-iterations/s",
                "h2d_bytes_per_step": 2 * cells * 8, "d2h_bytes_per_step": cells * 8,
                "ms_per_step": 1e3 * e_wall / args.steps,
                "ms_per_step_parts": {k: 1e3 * v / args.steps for k, v in
@@ -616,8 +600,7 @@ def main():
         }
         print(json.dumps(out), flush=True)
     chunk.close()
-    if dist is not None:
-        dist.destroy_process_group()
+    grp.close()
 
 
 if __name__ == "__main__":

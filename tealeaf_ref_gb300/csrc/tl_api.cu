@@ -80,6 +80,7 @@ struct tl_ctx {
   // CUDA graphs of one batch of the device-resident loops (captured once per set of kernel
   // arguments): the fused CG batch and the mixed-precision CG batch
   cudaGraphExec_t cg_exec = nullptr, mix_exec = nullptr;
+  int pgrid = -1;  // co-resident CTAs of the persistent CG kernel (-1: not yet queried)
   LoopArgs cg_key{};
   long long cg_nk = 0, mix_nk = 0;
   double prof_ms[TL_NUM_KERNEL_TIMERS] = {};
@@ -237,6 +238,23 @@ int capture_batch(tl_ctx* c, cudaGraphExec_t* exec, long long* nk, F&& launches)
 bool use_graphs() {
   const char* e = getenv("TL_NO_GRAPHS");
   return !(e && e[0] == '1');
+}
+
+// The persistent CG kernel replaces the batched kernels up to this many cells (plain or
+// jac_diag preconditioner): per iteration it measured 13.8 / 16.9 / 27.6 / 49.5 us at 128^2 /
+// 256^2 / 512^2 / 1024^2 against 25.6 / 26.2 / 32.3 / 47.6 us for the batched kernels (CUDA
+// graphs), so it stops paying near 800^2.  TL_CG_PERSISTENT=0 / 1 forces it off / on.
+constexpr long long PERSIST_MAX_CELLS = 640LL * 1024;
+constexpr int PERSIST_RUN = 256;  // iterations per launch at most (the host reads the status between)
+
+bool use_persistent(tl_ctx* c) {
+  if (c->prof || c->g.precond == TL_PREC_JAC_BLOCK) return false;
+  const char* e = getenv("TL_CG_PERSISTENT");
+  const bool forced_on = e && e[0] == '1', forced_off = e && e[0] == '0';
+  if (forced_off) return false;
+  if (!forced_on && (long long)c->L.nx * c->L.ny > PERSIST_MAX_CELLS) return false;
+  if (c->pgrid < 0) c->pgrid = persistent_cg_grid();
+  return c->pgrid > 0;
 }
 
 int run_cg_batch(tl_ctx* c, const LoopArgs& la) {
@@ -1196,7 +1214,12 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
       // device-resident CG loop, batches of iterations, one status read per batch
       LoopArgs la = c->loop();
       const int n_before = n;
-      if (!c->prof && use_graphs()) {
+      if (use_persistent(c)) {
+        launch_flush_u(la, c->stream);  // a pending update of the batched kernels (none normally)
+        unsigned* bar = c->counter + 4;  // barrier counter, generation, error word
+        CK(cudaMemsetAsync(bar, 0, 3 * sizeof(unsigned), c->stream));
+        CK(launch_persistent_cg(la, PERSIST_RUN, bar, c->pgrid, c->stream));
+      } else if (!c->prof && use_graphs()) {
         if ((rc = run_cg_batch(c, la))) return rc;
       } else {
         for (int i = 0; i < batch; ++i) {
@@ -1226,6 +1249,8 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
       }
       cg_calc_steps = H.cg_calc_steps;
       if (H.status == EXIT_BREAKDOWN) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite CG scalar");
+      if (H.status == EXIT_TIMEOUT)
+        return fail(TL_ERR_TIMEOUT, "tl_tea_leaf: a grid-barrier wait of the persistent CG kernel expired");
       if (H.status != RUN) {
         // the CG phase stops here: apply the deferred u += alpha p of its last iteration
         launch_flush_u(la, c->stream);

@@ -43,6 +43,7 @@ enum : int {
   EXIT_BREAKDOWN = 2,
   EXIT_MAX_ITERS = 3,
   STOP_SWITCH = 4,  // CG presteps done: host computes eigenvalues / coefficients
+  EXIT_TIMEOUT = 5, // a bounded grid-barrier wait of the persistent CG kernel expired
 };
 
 // Device-resident state of one tea_leaf() solve (tea_solve.f90:42-68).  Written only by

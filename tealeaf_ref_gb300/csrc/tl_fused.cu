@@ -230,6 +230,164 @@ __global__ void __launch_bounds__(FT) k_fused_cg_w(LoopArgs a, int rows_per_cta)
   grid_reduce<2>(acc, a.rd, EpiCgW{a.rd, PPCG});
 }
 
+// ---- persistent cooperative CG (small meshes) ----------------------------------------------
+// One cooperative launch runs up to `max_run` iterations of the CG loop (tea_solve.f90:341-369)
+// with grid barriers instead of kernel boundaries; the launch and reduction latency of two
+// kernels per iteration dominates below about a million cells.  Per iteration:
+//   phase A  p_n = src + beta p_{n-1} (neighbours' p_n recomputed in place), w = A p_n, p.w;
+//   barrier; every CTA sums the per-CTA partials in the same fixed order -> alpha;
+//   phase B  u += alpha p_n, r -= alpha w (z = Mi r for jac_diag), r.z;
+//   barrier; every CTA sums -> beta, error, the EXIT / switch tests of finish_iteration.
+// Each CTA runs the epilogues on its own shared-memory copy of the loop state (the sums are
+// identical, so are the decisions); CTA 0 writes the alpha/beta history and, at the end, the
+// state.  u is updated in phase B, so no update is left pending.
+// The grid barrier is an arrival counter and a generation word; a wait gives up after
+// PB_SPIN_LIMIT polls (about a second), sets the error word, and every CTA returns with
+// status EXIT_TIMEOUT instead of waiting longer.
+constexpr int PB_T = 256;
+constexpr unsigned long long PB_SPIN_LIMIT = 1ull << 24;
+
+__device__ __forceinline__ bool pb_barrier(unsigned* arrive, unsigned* gen, unsigned* err, unsigned nblocks) {
+  __shared__ int failed;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    failed = 0;
+    const unsigned g = atomicAdd(gen, 0u);
+    __threadfence();
+    if (atomicAdd(arrive, 1u) == nblocks - 1) {
+      atomicExch(arrive, 0u);
+      __threadfence();
+      atomicAdd(gen, 1u);
+    } else {
+      unsigned long long spins = 0;
+      while (atomicAdd(gen, 0u) == g) {
+        if (atomicAdd(err, 0u) != 0u || ++spins > PB_SPIN_LIMIT) {
+          atomicExch(err, 1u);
+          failed = 1;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return failed == 0;
+}
+
+// sum of partials[0 .. nb) in a fixed order; the same bits in every CTA
+__device__ __forceinline__ double pb_total(const double* partials, int nb, double* scratch, double* bcast) {
+  double v[1] = {0.0};
+  for (int b = threadIdx.x; b < nb; b += PB_T) v[0] += __ldcg(partials + b);
+  block_sum<1>(v, scratch);
+  if (threadIdx.x == 0) *bcast = v[0];
+  __syncthreads();
+  return *bcast;
+}
+
+__global__ void __launch_bounds__(PB_T) k_persistent_cg(LoopArgs a, int max_run, unsigned* bar) {
+  __shared__ LoopState S;
+  __shared__ double scratch[32];
+  __shared__ double bcast;
+  const Layout L = a.L;
+  const unsigned nb = gridDim.x;
+  unsigned* arrive = bar;
+  unsigned* gen = bar + 1;
+  unsigned* err = bar + 2;
+  if (threadIdx.x == 0) S = *a.rd.st;
+  __syncthreads();
+  const bool use_z = a.precond != 1;
+  const double* __restrict__ src = use_z ? a.f.z : a.f.r;
+  const long long ncell = (long long)L.nx * L.ny;
+  const long long stride = (long long)nb * PB_T;
+  double* partA = a.rd.partials;
+  double* partB = a.rd.partials + nb;
+  int done = 0;
+  bool ok = true;
+  while (S.status == RUN && done < max_run) {
+    const int n = S.n;
+    const double* __restrict__ pold = (n & 1) ? a.f.p : a.f.p2;
+    double* __restrict__ pout = (n & 1) ? a.f.p2 : a.f.p;
+    const bool upd = S.p_pending != 0;
+    const double beta = S.beta;
+    auto pn = [&](long long c) { return upd ? fma(beta, pold[c], src[c]) : pold[c]; };
+    // ---- phase A: p_n, w = A p_n, p.w ----
+    double acc[1] = {0.0};
+    for (long long i = (long long)blockIdx.x * PB_T + threadIdx.x; i < ncell; i += stride) {
+      const int j = (int)(i % L.nx) + 1, k = (int)(i / L.nx) + 1;
+      const long long c = L.at(j, k);
+      const double pc = pn(c);
+      // off the domain the neighbour is the mirror value (tl_fused.cu's matvec)
+      const double pt = k < L.ny ? pn(c + L.ld) : pc, pb = k > 1 ? pn(c - L.ld) : pc;
+      const double pr = j < L.nx ? pn(c + 1) : pc, pl = j > 1 ? pn(c - 1) : pc;
+      double wv = a.f.di[c] * pc;
+      wv = fma(-a.f.cy[c + L.ld], pt, wv);
+      wv = fma(-a.f.cy[c], pb, wv);
+      wv = fma(-a.f.cx[c + 1], pr, wv);
+      wv = fma(-a.f.cx[c], pl, wv);
+      a.f.w[c] = wv;
+      pout[c] = pc;
+      acc[0] = fma(wv, pc, acc[0]);
+    }
+    block_sum<1>(acc, scratch);
+    if (threadIdx.x == 0) partA[blockIdx.x] = acc[0];
+    __threadfence();
+    if (!(ok = pb_barrier(arrive, gen, err, nb))) break;
+    const double pw = pb_total(partA, nb, scratch, &bcast);
+    // EpiCgW
+    const double alpha = S.rro / pw;
+    if (threadIdx.x == 0) {
+      S.u_pending = 0;
+      S.pw = pw;
+      S.alpha = alpha;
+      if (blockIdx.x == 0) a.rd.hist_a[n] = alpha;
+      if (!isfinite(alpha)) {
+        S.status = EXIT_BREAKDOWN;
+        S.n_exit = n;
+      }
+    }
+    __syncthreads();
+    if (S.status != RUN) break;
+    // ---- phase B: u += alpha p_n, r -= alpha w, r.z ----
+    acc[0] = 0.0;
+    for (long long i = (long long)blockIdx.x * PB_T + threadIdx.x; i < ncell; i += stride) {
+      const int j = (int)(i % L.nx) + 1, k = (int)(i / L.nx) + 1;
+      const long long c = L.at(j, k);
+      a.f.u[c] = fma(alpha, pout[c], a.f.u[c]);
+      const double rv = fma(-alpha, a.f.w[c], a.f.r[c]);
+      a.f.r[c] = rv;
+      double zv = rv;
+      if (use_z) {
+        zv = a.f.mi[c] * rv;
+        a.f.z[c] = zv;
+      }
+      acc[0] = fma(rv, zv, acc[0]);
+    }
+    block_sum<1>(acc, scratch);
+    if (threadIdx.x == 0) partB[blockIdx.x] = acc[0];
+    __threadfence();
+    if (!(ok = pb_barrier(arrive, gen, err, nb))) break;
+    const double rrn = pb_total(partB, nb, scratch, &bcast);
+    // EpiCgUr (u already updated)
+    if (threadIdx.x == 0) {
+      S.rrn = rrn;
+      const double b = rrn / S.rro;
+      S.beta = b;
+      if (blockIdx.x == 0) a.rd.hist_b[n] = b;
+      S.p_pending = 1;
+      S.rro = rrn;
+      S.cg_calc_steps += 1;
+      finish_iteration(&S, rrn);
+    }
+    __syncthreads();
+    ++done;
+  }
+  if (!ok && threadIdx.x == 0) S.status = EXIT_TIMEOUT;
+  __syncthreads();
+  // every CTA's copy is the same; CTA 0 publishes it (after all CTAs read the state at entry)
+  if (blockIdx.x == 0 && threadIdx.x == 0) *a.rd.st = S;
+}
+
 // Applies a pending deferred u update (LoopState::u_pending) when the CG loop stops.
 __global__ void __launch_bounds__(FT) k_flush_u(LoopArgs a) {
   const LoopState* st = a.rd.st;
@@ -367,6 +525,25 @@ void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s) {
     { ++launch_counter(); k_fused_cg_w<true><<<grid, FT, 0, s>>>(a, rows); }
   else
     { ++launch_counter(); k_fused_cg_w<false><<<grid, FT, 0, s>>>(a, rows); }
+}
+
+int persistent_cg_grid() {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent_cg, PB_T, 0) != cudaSuccess) return 0;
+  return sms * per_sm;
+}
+
+cudaError_t launch_persistent_cg(const LoopArgs& a, int max_run, unsigned* bar, int grid, cudaStream_t s) {
+  const long long ncell = (long long)a.L.nx * a.L.ny;
+  long long need = (ncell + PB_T - 1) / PB_T;
+  int g = (int)(need < grid ? need : grid);
+  if (g < 1) g = 1;
+  LoopArgs aa = a;
+  void* args[] = {&aa, &max_run, &bar};
+  ++launch_counter();
+  return cudaLaunchCooperativeKernel((const void*)k_persistent_cg, dim3(g), dim3(PB_T), args, 0, s);
 }
 
 void launch_fused_cg_ur(const LoopArgs& a, bool ppcg, cudaStream_t s) {

@@ -75,6 +75,11 @@ void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s);
 void launch_fused_cg_ur(const LoopArgs& a, bool ppcg, cudaStream_t s);
 // u += alpha p of the last CG iteration when it is still pending (end of a CG phase)
 void launch_flush_u(const LoopArgs& a, cudaStream_t s);
+// persistent cooperative CG (no preconditioner or jac_diag): up to max_run iterations in one
+// launch; bar = three zeroed words (barrier counter, generation, error); grid = the co-resident
+// CTA count from persistent_cg_grid() (0 if it cannot be determined)
+int persistent_cg_grid();
+cudaError_t launch_persistent_cg(const LoopArgs& a, int max_run, unsigned* bar, int grid, cudaStream_t s);
 // one Jacobi iteration from un into u_out (the two swap every iteration), error and the loop's
 // test in the epilogue
 void launch_fused_jacobi(const LoopArgs& a, const double* un, double* u_out, cudaStream_t s);

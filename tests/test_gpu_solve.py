@@ -129,3 +129,29 @@ def test_breakdown_reported():
         with pytest.raises(native.TeaLeafError) as e:
             c.tea_leaf(d)
         assert e.value.code == -4
+
+
+@pytest.mark.parametrize("case", [dict(), dict(precond="jac_diag"), dict(reflective=True),
+                                  dict(solver="ppcg", ppcg_inner_steps=8, ch_cg_presteps=20)],
+                         ids=["cg", "jac_diag", "reflective", "ppcg-presteps"])
+def test_persistent_cg_matches_batched(case, monkeypatch):
+    """The persistent cooperative CG kernel (one launch for many iterations, grid barriers)
+    against the batched fused kernels on the same deck: field summary 1e-10, u 1e-8, iteration
+    counts within a few (different reduction trees)."""
+    from tealeaf_ref_gb300 import native
+
+    kw = dict(nx=203, ny=151, steps=3, n_rect=4, n_circ=2, max_iters=20000)
+    kw.update(case)
+    d = small_deck(**kw)
+    runs = []
+    for forced in ("0", "1"):
+        monkeypatch.setenv("TL_CG_PERSISTENT", forced)
+        with native.Chunk.from_deck(d) as c:
+            its = [c.tea_leaf(d).reported_iterations for _ in range(d.end_step)]
+            runs.append((c.field_summary(), c.download("u"), its))
+    (s0, u0, i0), (s1, u1, i1) = runs
+    ok, worst = _summary_close(s1, s0, 1e-10)
+    assert ok, worst
+    assert np.max(np.abs(u1 - u0) / np.abs(u0)) < 1e-8
+    for a, b in zip(i1, i0):
+        assert abs(a - b) <= max(2, int(0.01 * b)), (i1, i0)

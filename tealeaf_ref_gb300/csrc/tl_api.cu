@@ -1218,7 +1218,11 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
         launch_flush_u(la, c->stream);  // a pending update of the batched kernels (none normally)
         unsigned* bar = c->counter + 4;  // barrier counter, generation, error word
         CK(cudaMemsetAsync(bar, 0, 3 * sizeof(unsigned), c->stream));
-        CK(launch_persistent_cg(la, PERSIST_RUN, bar, c->pgrid, c->stream));
+        // TL_CG_BARRIER_EXTRA=1: the barriers wait for one arrival that never comes, so every
+        // wait runs out (about a second) and the solve reports TL_ERR_TIMEOUT -- the test of the
+        // bounded wait
+        const char* ex = getenv("TL_CG_BARRIER_EXTRA");
+        CK(launch_persistent_cg(la, PERSIST_RUN, bar, c->pgrid, c->stream, ex && ex[0] == '1' ? 1 : 0));
       } else if (!c->prof && use_graphs()) {
         if ((rc = run_cg_batch(c, la))) return rc;
       } else {

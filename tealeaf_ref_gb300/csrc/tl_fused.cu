@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(FT) k_fused_cg_w(LoopArgs a, int rows_per_cta)
 // PB_SPIN_LIMIT polls (about a second), sets the error word, and every CTA returns with
 // status EXIT_TIMEOUT instead of waiting longer.
 constexpr int PB_T = 256;
-constexpr unsigned long long PB_SPIN_LIMIT = 1ull << 24;
+constexpr unsigned long long PB_SPIN_LIMIT = 1ull << 22;  // polls of >= 64 ns plus two L2 atomics each
 
 __device__ __forceinline__ bool pb_barrier(unsigned* arrive, unsigned* gen, unsigned* err, unsigned nblocks) {
   __shared__ int failed;
@@ -285,12 +285,15 @@ __device__ __forceinline__ double pb_total(const double* partials, int nb, doubl
   return *bcast;
 }
 
-__global__ void __launch_bounds__(PB_T) k_persistent_cg(LoopArgs a, int max_run, unsigned* bar) {
+// extra_arrivals: arrivals the barriers wait for beyond the grid's CTAs -- 0, except in the test
+// of the bounded wait (an arrival that never comes)
+__global__ void __launch_bounds__(PB_T) k_persistent_cg(LoopArgs a, int max_run, unsigned* bar, int extra_arrivals) {
   __shared__ LoopState S;
   __shared__ double scratch[32];
   __shared__ double bcast;
   const Layout L = a.L;
   const unsigned nb = gridDim.x;
+  const unsigned nwait = nb + (unsigned)extra_arrivals;
   unsigned* arrive = bar;
   unsigned* gen = bar + 1;
   unsigned* err = bar + 2;
@@ -332,7 +335,7 @@ __global__ void __launch_bounds__(PB_T) k_persistent_cg(LoopArgs a, int max_run,
     block_sum<1>(acc, scratch);
     if (threadIdx.x == 0) partA[blockIdx.x] = acc[0];
     __threadfence();
-    if (!(ok = pb_barrier(arrive, gen, err, nb))) break;
+    if (!(ok = pb_barrier(arrive, gen, err, nwait))) break;
     const double pw = pb_total(partA, nb, scratch, &bcast);
     // EpiCgW
     const double alpha = S.rro / pw;
@@ -366,7 +369,7 @@ __global__ void __launch_bounds__(PB_T) k_persistent_cg(LoopArgs a, int max_run,
     block_sum<1>(acc, scratch);
     if (threadIdx.x == 0) partB[blockIdx.x] = acc[0];
     __threadfence();
-    if (!(ok = pb_barrier(arrive, gen, err, nb))) break;
+    if (!(ok = pb_barrier(arrive, gen, err, nwait))) break;
     const double rrn = pb_total(partB, nb, scratch, &bcast);
     // EpiCgUr (u already updated)
     if (threadIdx.x == 0) {
@@ -535,13 +538,14 @@ int persistent_cg_grid() {
   return sms * per_sm;
 }
 
-cudaError_t launch_persistent_cg(const LoopArgs& a, int max_run, unsigned* bar, int grid, cudaStream_t s) {
+cudaError_t launch_persistent_cg(const LoopArgs& a, int max_run, unsigned* bar, int grid, cudaStream_t s,
+                                 int extra_arrivals) {
   const long long ncell = (long long)a.L.nx * a.L.ny;
   long long need = (ncell + PB_T - 1) / PB_T;
   int g = (int)(need < grid ? need : grid);
   if (g < 1) g = 1;
   LoopArgs aa = a;
-  void* args[] = {&aa, &max_run, &bar};
+  void* args[] = {&aa, &max_run, &bar, &extra_arrivals};
   ++launch_counter();
   return cudaLaunchCooperativeKernel((const void*)k_persistent_cg, dim3(g), dim3(PB_T), args, 0, s);
 }

@@ -79,7 +79,8 @@ void launch_flush_u(const LoopArgs& a, cudaStream_t s);
 // launch; bar = three zeroed words (barrier counter, generation, error); grid = the co-resident
 // CTA count from persistent_cg_grid() (0 if it cannot be determined)
 int persistent_cg_grid();
-cudaError_t launch_persistent_cg(const LoopArgs& a, int max_run, unsigned* bar, int grid, cudaStream_t s);
+cudaError_t launch_persistent_cg(const LoopArgs& a, int max_run, unsigned* bar, int grid, cudaStream_t s,
+                                 int extra_arrivals = 0);
 // one Jacobi iteration from un into u_out (the two swap every iteration), error and the loop's
 // test in the epilogue
 void launch_fused_jacobi(const LoopArgs& a, const double* un, double* u_out, cudaStream_t s);

@@ -155,3 +155,26 @@ def test_persistent_cg_matches_batched(case, monkeypatch):
     assert np.max(np.abs(u1 - u0) / np.abs(u0)) < 1e-8
     for a, b in zip(i1, i0):
         assert abs(a - b) <= max(2, int(0.01 * b)), (i1, i0)
+
+
+def test_persistent_cg_barrier_wait_is_bounded(monkeypatch):
+    """The persistent kernel's grid-barrier waits end by themselves: made to wait for an
+    arrival that never comes, every CTA gives up after about a second, the solve returns
+    TL_ERR_TIMEOUT, and the context solves normally afterwards."""
+    import time
+
+    from tealeaf_ref_gb300 import native
+
+    d = small_deck(nx=64, ny=64, steps=1, n_rect=2, n_circ=1)
+    monkeypatch.setenv("TL_CG_PERSISTENT", "1")
+    with native.Chunk.from_deck(d) as c:
+        monkeypatch.setenv("TL_CG_BARRIER_EXTRA", "1")
+        t0 = time.perf_counter()
+        with pytest.raises(native.TeaLeafError) as e:
+            c.tea_leaf(d)
+        assert e.value.code == -5  # TL_ERR_TIMEOUT
+        assert time.perf_counter() - t0 < 60
+        monkeypatch.delenv("TL_CG_BARRIER_EXTRA")
+        c.generate(d)
+        info = c.tea_leaf(d)
+        assert info.reported_iterations > 0

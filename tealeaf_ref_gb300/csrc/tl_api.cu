@@ -837,7 +837,7 @@ int ensure_mix(tl_ctx* c) {
   float* b = reinterpret_cast<float*>(c->mix_slab);
   const size_t step = fb / sizeof(float);
   c->mix = MixFields{b,            b + step,     b + 2 * step, b + 3 * step, b + 4 * step,
-                     b + 5 * step, b + 6 * step, b + 7 * step, b + 8 * step};
+                     b + 5 * step, b + 6 * step, b + 7 * step, b + 8 * step, c->counter + 8};
   CK(cudaMalloc(&c->mst, sizeof(MixState)));
   CK(cudaMallocHost(&c->mst_host, sizeof(MixState)));
   if (prepare_mix_kernels() != 0) return fail(TL_ERR_CUDA, "cannot set the mixed-precision kernels' shared memory");
@@ -1424,6 +1424,18 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
     launch_residual(c->f, c->L, &rd, RED_STORE, c->stream);
     if ((rc = reduce_result(c, &exact_error))) return rc;
     exact_error = std::sqrt(exact_error);
+  }
+  if (mixed) {
+    // a blocked FP32 sweep sets this word when a staged row did not arrive within its bounded
+    // wait (1) or its shared memory was misaligned for TMA (2)
+    unsigned werr = 0;
+    CK(cudaMemcpyAsync(&werr, c->mix.err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (werr) {
+      CK(cudaMemsetAsync(c->mix.err, 0, sizeof(unsigned), c->stream));
+      return fail(TL_ERR_TIMEOUT, werr == 1 ? "tl_tea_leaf: a staged row of a blocked FP32 sweep did not arrive in time"
+                                            : "tl_tea_leaf: shared memory misaligned for the blocked FP32 sweep");
+    }
   }
   if (finalise) {
     launch_finalise(c->f, c->L, c->stream);

@@ -91,6 +91,7 @@ struct MixFields {
   float *cx, *cy, *di;  // FP32 copies of the pre-scaled operator
   float *r, *p, *p2, *w, *d;
   float* e;             // second buffer of the blocked polynomial sweeps' ping-pong
+  unsigned* err;        // set by a blocked sweep whose bounded wait for a staged row expired
 };
 struct MixState {
   double rro, rro_prev, pw, rr, alpha, beta;  // FP32-vector CG scalars (FP64)

@@ -8,7 +8,14 @@
 // PPCG uses r = rtemp, p / p2 = sd (ping-pong), w = utemp; Chebyshev uses r = its right-hand
 // side, p = its direction, d / p2 = the correction (ping-pong, ending in d).  Off-domain
 // neighbours: see apply_a32 (with zero boundary coefficients either choice gives the same).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "tl_kernels.cuh"
 
@@ -165,7 +172,15 @@ struct PolyArgs {
   float inv_theta;
   int first;           // level 0 synthesised: PPCG init_sd from r64, Chebyshev start from m.r
   int rows, nstrips, ntasks;
+  int tx, t1, t2;      // TMA: indices in PolyMaps of the maps of x_in, c1_in, c2_in
   float ca[TB_S], cb[TB_S];
+};
+
+// Tensor maps (TMA descriptors) of the fields a blocked sweep reads: each a 2-D view
+// (ld x (ny+2)) with a 128-element by 1-row box.
+enum { PM_P = 0, PM_P2, PM_R, PM_W, PM_D, PM_E, PM_CX, PM_CY, PM_DI, PM_R64, PM_N };
+struct PolyMaps {
+  CUtensorMap t[PM_N];
 };
 
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
@@ -184,14 +199,56 @@ __device__ __forceinline__ void store4(float* __restrict__ p, long long c, const
 
 // Per-warp shared memory of the blocked sweep: a ring of RING coefficient rows (di, cx, cy, and
 // Chebyshev's right-hand side; 132 floats per array row) and a ring of TB_P+1 input-state rows.
-template <int MODE, int S>
+// With TMA the array rows are 128 floats apart (every TMA destination 128-byte aligned; the
+// lane that reads column j+4 past its warp's strip is a halo lane) and TB_P+1 mbarriers follow.
+template <int MODE, int S, bool TMA>
 struct TbSmem {
   static constexpr int NC = MODE == POLY_PPCG ? 3 : 4;
   static constexpr int RING = S + 1 + TB_P;
+  static constexpr int CP = TMA ? 128 : 132;                          // floats per coefficient array row
   static constexpr int SSLOT = (MODE == POLY_PPCG ? 3 : 2) * 128;  // floats (PPCG: or 128 doubles)
-  static constexpr int WARP_FLOATS = RING * NC * 132 + (TB_P + 1) * SSLOT;
+  static constexpr int BAR = TMA ? 32 : 0;                          // floats: the mbarriers (128 B)
+  static constexpr int WARP_FLOATS = RING * NC * CP + (TB_P + 1) * SSLOT + BAR;
   static constexpr int BYTES = TB_WARPS * WARP_FLOATS * 4;
 };
+
+constexpr unsigned long long TB_WAIT_LIMIT = 1ull << 24;  // polls of a staged row (>= 32 ns each)
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// bounded wait for the phase with the given parity to complete; false if it did not
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  const unsigned a = smem_u32(bar);
+  for (unsigned long long i = 0; i < TB_WAIT_LIMIT; ++i) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    __nanosleep(32);
+  }
+  return false;
+}
+// one 128-element row box of a 2-D tensor map into shared memory, completing on bar
+__device__ __forceinline__ void tma_row(void* dst, const CUtensorMap* map, int x, int y, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
 
 __device__ __forceinline__ void cp_async16(float* dst, const void* src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -221,11 +278,11 @@ __device__ __forceinline__ void stage4d(double* dst, const double* __restrict__ 
   }
 }
 
-template <int MODE, int S>
-__global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
+template <int MODE, int S, bool TMA>
+__global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __grid_constant__ PolyMaps pm) {
   constexpr bool PPCG = MODE == POLY_PPCG;
-  using SM = TbSmem<MODE, S>;
-  constexpr int NC = SM::NC, RING = SM::RING;
+  using SM = TbSmem<MODE, S, TMA>;
+  constexpr int NC = SM::NC, RING = SM::RING, CP = SM::CP;
   const int lane = threadIdx.x & 31;
   const int task = blockIdx.x * TB_WARPS + (threadIdx.x >> 5);
   if (task >= a.ntasks) return;  // whole warps only
@@ -237,17 +294,68 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
   const int j = x0 - TB_HX + 4 * lane;  // this lane's first column
   const int out0 = x0, out1 = min(x0 + TB_W - 1, L.nx);
   const int lc = 4 * lane;
-  extern __shared__ __align__(16) float tb_smem[];
+  extern __shared__ __align__(128) float tb_smem[];
   float* const wbase = tb_smem + (threadIdx.x >> 5) * SM::WARP_FLOATS;
   // ring slots: row r sits in coefficient slot (r - mstart) mod RING and state slot
   // (r - mstart) mod (TB_P+1); the march keeps the slots of row mm in running counters
-  auto coef = [&](int slot, int arr) { return wbase + (slot * NC + arr) * 132; };
-  auto state = [&](int slot, int arr) { return wbase + RING * NC * 132 + slot * SM::SSLOT + arr * 128; };
+  auto coef = [&](int slot, int arr) { return wbase + (slot * NC + arr) * CP; };
+  auto state = [&](int slot, int arr) { return wbase + RING * NC * CP + slot * SM::SSLOT + arr * 128; };
   constexpr int SR = TB_P + 1;
+  unsigned long long* const bars =
+      reinterpret_cast<unsigned long long*>(wbase + RING * NC * CP + SR * SM::SSLOT);  // TMA: one per state slot
   const int crow_max = min(L.ny + 1, k1 + S);  // coefficient rows (cy also of the boundary row ny+1)
   const int srow_max = min(L.ny, k1 + S);      // input-state rows
+  const int tmx = (XOFF - 1) + (x0 - TB_HX);  // TMA: first element of the warp's strip in a row
+  if (TMA) {
+    if (smem_u32(tb_smem) & 127u) {  // TMA destinations must be 128-byte aligned
+      if (lane == 0) atomicExch(a.m.err, 2u);
+      return;
+    }
+    if (lane == 0)
+      for (int b = 0; b < SR; ++b) mbar_init(&bars[b], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncwarp();
+  }
+  // TMA: one lane arms the row's mbarrier with the byte count and issues the row's tensor copies
+  // (columns past the field's rows read as zero); an empty row only arrives
+  auto issue_row_tma = [&](int row, int cs, int ss) {
+    if (lane != 0) return;
+    unsigned bytes = 0;
+    if (row <= crow_max) bytes += (row <= L.ny ? (PPCG ? 3 : 4) : 1) * 512;
+    if (row <= srow_max) bytes += a.first ? (PPCG ? 1024 : 0) : (PPCG ? 3 : 2) * 512;
+    unsigned long long* bar = &bars[ss];
+    if (bytes == 0) {
+      mbar_arrive(bar);
+      return;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the lanes' reads of these slots come first
+    mbar_expect_tx(bar, bytes);
+    if (row <= crow_max) {
+      tma_row(coef(cs, 2), &pm.t[PM_CY], tmx, row, bar);
+      if (row <= L.ny) {
+        tma_row(coef(cs, 0), &pm.t[PM_DI], tmx, row, bar);
+        tma_row(coef(cs, 1), &pm.t[PM_CX], tmx, row, bar);
+        if (!PPCG) tma_row(coef(cs, 3), &pm.t[PM_R], tmx, row, bar);
+      }
+    }
+    if (row <= srow_max) {
+      if (a.first) {
+        if (PPCG) tma_row(state(ss, 0), &pm.t[PM_R64], tmx, row, bar);
+      } else {
+        tma_row(state(ss, 0), &pm.t[a.tx], tmx, row, bar);
+        tma_row(state(ss, 1), &pm.t[a.t1], tmx, row, bar);
+        if (PPCG) tma_row(state(ss, 2), &pm.t[a.t2], tmx, row, bar);
+      }
+    }
+  };
+  unsigned parity = 0;  // TMA: bit b = phase parity of mbarrier b's next completion
+  bool stalled = false;
   // stage row `row` (coefficients and input state) into the rings; one commit group per row
   auto issue_row = [&](int row, int cs, int ss) {
+    if (TMA) {
+      issue_row_tma(row, cs, ss);
+      return;
+    }
     if (row <= crow_max) {
       const long long c = L.at(j, row);
       stage4(coef(cs, 2) + lc, m.cy + c, j, 1, L.nx);
@@ -306,7 +414,21 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
       prefetch_l2(m.cy + c);
       if (!PPCG) prefetch_l2(m.r + c);
     }
-    cp_async_wait<TB_P>();  // row mm has landed
+    if (TMA) {
+      // row mm has landed: lane 0 polls (bounded) and tells the warp, so the warp stays
+      // converged whatever happens; each lane then observes the completed phase itself
+      int ok = lane == 0 ? (int)mbar_wait(&bars[sslot], (parity >> sslot) & 1u) : 0;
+      ok = __shfl_sync(FULL, ok, 0);
+      if (!ok) {
+        stalled = true;
+        if (lane == 0) atomicExch(a.m.err, 1u);
+        break;
+      }
+      mbar_wait(&bars[sslot], (parity >> sslot) & 1u);  // completes at the first poll
+      parity ^= 1u << sslot;
+    } else {
+      cp_async_wait<TB_P>();  // row mm has landed
+    }
     __syncwarp();
     // ---- level 0: the sweep's input at row mm ----
     float nx[4] = {0.f, 0.f, 0.f, 0.f}, n1[4] = {0.f, 0.f, 0.f, 0.f}, n2[4] = {0.f, 0.f, 0.f, 0.f};
@@ -431,7 +553,14 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a) {
     if (++cslot == RING) cslot = 0;
     if (++sslot == SR) sslot = 0;
   }
-  cp_async_wait<0>();  // no copy outstanding when the warp exits
+  if (TMA) {
+    // every copy issued was for a row the march waited for, unless a wait expired: then give
+    // the others in flight a bounded time to land before the warp's shared memory is released
+    if (stalled && lane == 0)
+      for (int b = 0; b < SR; ++b) mbar_wait(&bars[b], (parity >> b) & 1u);
+  } else {
+    cp_async_wait<0>();  // no copy outstanding when the warp exits
+  }
 }
 
 // Steps per blocked sweep: TB_S, or TL_POLY_STEPS_PER_SWEEP (1 .. TB_S) from the environment;
@@ -453,23 +582,108 @@ void tb_tasks(PolyArgs& a, const Layout& L) {
   a.ntasks = a.nstrips * ((L.ny + rows - 1) / rows);
 }
 
-template <int MODE, int S>
-void launch_tb_s(const PolyArgs& a, dim3 grid, cudaStream_t s) {
-  constexpr int bytes = TbSmem<MODE, S>::BYTES;
+template <int MODE, int S, bool TMA>
+void launch_tb_s(const PolyArgs& a, const PolyMaps& pm, dim3 grid, cudaStream_t s) {
+  constexpr int bytes = TbSmem<MODE, S, TMA>::BYTES;
   // above the 48 KB default: the attribute is set on the current device before each launch
-  cudaFuncSetAttribute(k_poly_tb<MODE, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  k_poly_tb<MODE, S><<<grid, 32 * TB_WARPS, bytes, s>>>(a);
+  cudaFuncSetAttribute(k_poly_tb<MODE, S, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  k_poly_tb<MODE, S, TMA><<<grid, 32 * TB_WARPS, bytes, s>>>(a, pm);
+}
+
+// ---- tensor maps ----
+// TL_POLY_TMA=0 stages with cp.async instead of TMA (same results, bit for bit).
+bool poly_use_tma() {
+  const char* e = getenv("TL_POLY_TMA");
+  return !(e && e[0] == '0');
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// a (ld x (ny+2)) view of one field with a 128 x 1 box; cached per (address, layout, type)
+bool tmap_of(const void* base, const Layout& L, bool f64, CUtensorMap* out) {
+  static std::mutex mu;
+  static std::map<std::tuple<const void*, int, int, bool>, CUtensorMap> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_tuple(base, L.ld, L.ny, f64);
+  auto it = cache.find(key);
+  if (it != cache.end()) {
+    *out = it->second;
+    return true;
+  }
+  auto enc = tmap_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)L.ld, (cuuint64_t)L.ny + 2};
+  const cuuint64_t strides[1] = {(cuuint64_t)L.ld * (f64 ? 8 : 4)};
+  const cuuint32_t box[2] = {128, 1};
+  const cuuint32_t estr[2] = {1, 1};
+  CUtensorMap m;
+  if (enc(&m, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims,
+          strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  cache[key] = m;
+  *out = m;
+  return true;
+}
+
+// the maps of every field a blocked sweep may read; false if TMA is off or unavailable
+bool poly_maps(const MixFields& m, const Layout& L, const double* r64, PolyMaps* pm) {
+  if (!poly_use_tma()) return false;
+  const float* f[PM_R64] = {m.p, m.p2, m.r, m.w, m.d, m.e, m.cx, m.cy, m.di};
+  for (int i = 0; i < PM_R64; ++i)
+    if (!tmap_of(f[i], L, false, &pm->t[i])) return false;
+  if (r64) {
+    if (!tmap_of(r64, L, true, &pm->t[PM_R64])) return false;
+  } else {
+    pm->t[PM_R64] = pm->t[PM_R];  // not read
+  }
+  return true;
+}
+
+int map_index(const MixFields& m, const float* p) {
+  if (p == m.p) return PM_P;
+  if (p == m.p2) return PM_P2;
+  if (p == m.r) return PM_R;
+  if (p == m.w) return PM_W;
+  if (p == m.d) return PM_D;
+  if (p == m.e) return PM_E;
+  return PM_R;  // (the first sweep reads no state map)
 }
 
 template <int MODE>
-void launch_tb(const PolyArgs& a, int steps, cudaStream_t s) {
+void launch_tb(PolyArgs a, int steps, bool tma, const PolyMaps& pm, cudaStream_t s) {
   const dim3 grid((a.ntasks + TB_WARPS - 1) / TB_WARPS);
+  a.tx = map_index(a.m, a.x_in);
+  a.t1 = map_index(a.m, a.c1_in);
+  a.t2 = map_index(a.m, a.c2_in);
   ++launch_counter();
-  switch (steps) {
-    case 1: launch_tb_s<MODE, 1>(a, grid, s); break;
-    case 2: launch_tb_s<MODE, 2>(a, grid, s); break;
-    case 3: launch_tb_s<MODE, 3>(a, grid, s); break;
-    default: launch_tb_s<MODE, 4>(a, grid, s); break;
+  if (tma) {
+    switch (steps) {
+      case 1: launch_tb_s<MODE, 1, true>(a, pm, grid, s); break;
+      case 2: launch_tb_s<MODE, 2, true>(a, pm, grid, s); break;
+      case 3: launch_tb_s<MODE, 3, true>(a, pm, grid, s); break;
+      default: launch_tb_s<MODE, 4, true>(a, pm, grid, s); break;
+    }
+  } else {
+    switch (steps) {
+      case 1: launch_tb_s<MODE, 1, false>(a, pm, grid, s); break;
+      case 2: launch_tb_s<MODE, 2, false>(a, pm, grid, s); break;
+      case 3: launch_tb_s<MODE, 3, false>(a, pm, grid, s); break;
+      default: launch_tb_s<MODE, 4, false>(a, pm, grid, s); break;
+    }
   }
 }
 
@@ -486,6 +700,8 @@ void launch_poly_ppcg_inner(const Fields& f, const MixFields& m, const Layout& L
     a.r64 = f.r;
     a.inv_theta = (float)(1.0 / theta);
     tb_tasks(a, L);
+    PolyMaps pm;
+    const bool tma = poly_maps(m, L, f.r, &pm);
     int done = 0, par = 0;
     while (done < inner_steps) {
       const int st = inner_steps - done < blk ? inner_steps - done : blk;
@@ -501,7 +717,7 @@ void launch_poly_ppcg_inner(const Fields& f, const MixFields& m, const Layout& L
         a.cb[i] = i < st ? (float)ch_b[done + 1 + i] : 0.f;
       }
       a.z = done + st == inner_steps ? f.z : nullptr;
-      launch_tb<POLY_PPCG>(a, st, s);
+      launch_tb<POLY_PPCG>(a, st, tma, pm, s);
       done += st;
       par ^= 1;
     }
@@ -534,6 +750,8 @@ void launch_poly_cheby(const MixFields& m, const Layout& L, double theta, int st
     a.L = L;
     a.inv_theta = (float)(1.0 / theta);
     tb_tasks(a, L);
+    PolyMaps pm;
+    const bool tma = poly_maps(m, L, nullptr, &pm);
     const int nb = (iters + blk - 1) / blk;
     const float* din = nullptr;
     const float* pin = nullptr;
@@ -549,7 +767,7 @@ void launch_poly_cheby(const MixFields& m, const Layout& L, double theta, int st
         a.ca[i] = i < st ? (float)ch_a[b * blk + 1 + i] : 0.f;
         a.cb[i] = i < st ? (float)ch_b[b * blk + 1 + i] : 0.f;
       }
-      launch_tb<POLY_CHEBY>(a, st, s);
+      launch_tb<POLY_CHEBY>(a, st, tma, pm, s);
       din = a.x_out;
       pin = a.c1_out;
     }

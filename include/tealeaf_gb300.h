@@ -169,6 +169,22 @@ int tl_download_field(tl_ctx* ctx, int field, double* host, int ld);
  * every solve initialises what it reads. */
 int tl_upload_state(tl_ctx* ctx, const double* density, const double* energy1, int ld);
 
+/* Pipelined transfers (no counterpart in the reference): host copies that overlap the solves.
+ * tl_stage_state starts copying a (density, energy1) pair from page-locked host memory into one
+ * of two device staging slots and returns at once; the host arrays must stay unchanged until
+ * the pair has been taken and tl_wait_transfers has returned (or the next tl_take_staged of
+ * that slot has run).  At most two pairs are staged (TL_ERR_STATE beyond).
+ * tl_take_staged queues, ahead of the next solve, the move of the oldest staged pair into the
+ * fields (the device waits for its copy; reflective halos are primed); TL_ERR_STATE if none.
+ * tl_fetch_field snapshots a field after the work queued so far and copies the snapshot to
+ * host memory on a separate stream, returning at once; the host array is valid after
+ * tl_wait_transfers.  A typical step: take the staged pair, solve, fetch energy1, stage the
+ * pair for the step after next -- the copies then run during the solves. */
+int tl_stage_state(tl_ctx* ctx, const double* density, const double* energy1, int ld);
+int tl_take_staged(tl_ctx* ctx);
+int tl_fetch_field(tl_ctx* ctx, int field, double* host, int ld);
+int tl_wait_transfers(tl_ctx* ctx);
+
 /* ---- chunk generation and summary (generate_chunk, field_summary) -------- */
 
 /* generate_chunk_kernel.f90:80-140 + set_field_kernel.f90:41-47 on the device.

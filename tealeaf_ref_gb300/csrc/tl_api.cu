@@ -81,6 +81,14 @@ struct tl_ctx {
   // arguments): the fused CG batch and the mixed-precision CG batch
   cudaGraphExec_t cg_exec = nullptr, mix_exec = nullptr;
   int pgrid = -1;  // co-resident CTAs of the persistent CG kernel (-1: not yet queried)
+  // pipelined host transfers (tl_stage_state, tl_take_staged, tl_fetch_field): an upload and a
+  // download stream, two staging slots of (density, energy1) and one fetch snapshot
+  cudaStream_t up = nullptr, down = nullptr;
+  char* xfer = nullptr;
+  cudaEvent_t st_done[2] = {}, st_used[2] = {}, fe_snap = nullptr, fe_done = nullptr;
+  bool st_used_rec[2] = {false, false}, fe_done_rec = false;
+  int st_head = 0, st_count = 0;
+  double* xfield(int i) const { return reinterpret_cast<double*>(xfer + (size_t)i * field_stride); }
   LoopArgs cg_key{};
   long long cg_nk = 0, mix_nk = 0;
   double prof_ms[TL_NUM_KERNEL_TIMERS] = {};
@@ -502,6 +510,17 @@ int tl_destroy(tl_ctx* c) {
     if (c->pev[i]) cudaEventDestroy(c->pev[i]);
   if (c->qe0) cudaEventDestroy(c->qe0);
   if (c->qe1) cudaEventDestroy(c->qe1);
+  if (c->up) cudaStreamSynchronize(c->up);
+  if (c->down) cudaStreamSynchronize(c->down);
+  cudaFree(c->xfer);
+  for (int i = 0; i < 2; ++i) {
+    if (c->st_done[i]) cudaEventDestroy(c->st_done[i]);
+    if (c->st_used[i]) cudaEventDestroy(c->st_used[i]);
+  }
+  if (c->fe_snap) cudaEventDestroy(c->fe_snap);
+  if (c->fe_done) cudaEventDestroy(c->fe_done);
+  if (c->up) cudaStreamDestroy(c->up);
+  if (c->down) cudaStreamDestroy(c->down);
   if (c->cg_exec) cudaGraphExecDestroy(c->cg_exec);
   if (c->mix_exec) cudaGraphExecDestroy(c->mix_exec);
   cudaFree(c->tape);
@@ -565,6 +584,96 @@ int tl_upload_state(tl_ctx* c, const double* density, const double* energy1, int
     if (rc) return rc;
   }
   CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+}  // extern "C"
+
+namespace {
+int ensure_xfer(tl_ctx* c) {
+  if (c->xfer) return TL_OK;
+  CK(cudaStreamCreateWithFlags(&c->up, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&c->down, cudaStreamNonBlocking));
+  for (int i = 0; i < 2; ++i) {
+    CK(cudaEventCreateWithFlags(&c->st_done[i], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->st_used[i], cudaEventDisableTiming));
+  }
+  CK(cudaEventCreateWithFlags(&c->fe_snap, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&c->fe_done, cudaEventDisableTiming));
+  if (cudaMalloc(&c->xfer, 5 * c->field_stride) != cudaSuccess) {
+    cudaGetLastError();
+    c->xfer = nullptr;
+    return fail(TL_ERR_ALLOC, "cannot allocate the staging fields of the pipelined transfers");
+  }
+  CK(cudaMemsetAsync(c->xfer, 0, 5 * c->field_stride, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int tl_stage_state(tl_ctx* c, const double* density, const double* energy1, int ld) {
+  if (!c || !density || !energy1) return fail(TL_ERR_ARG, "tl_stage_state: null argument");
+  if (ld < c->L.nx) return fail(TL_ERR_ARG, "tl_stage_state: ld < x_cells");
+  int rc;
+  if ((rc = ensure_xfer(c))) return rc;
+  if (c->st_count == 2) return fail(TL_ERR_STATE, "tl_stage_state: two states are staged already");
+  const int slot = c->st_head;
+  if (c->st_used_rec[slot]) CK(cudaStreamWaitEvent(c->up, c->st_used[slot], 0));  // the slot's last take is done
+  const size_t dp = sizeof(double) * c->L.ld, sp = sizeof(double) * ld, w = sizeof(double) * c->L.nx;
+  CK(cudaMemcpy2DAsync(c->xfield(2 * slot) + c->L.at(1, 1), dp, density, sp, w, c->L.ny, cudaMemcpyHostToDevice,
+                       c->up));
+  CK(cudaMemcpy2DAsync(c->xfield(2 * slot + 1) + c->L.at(1, 1), dp, energy1, sp, w, c->L.ny,
+                       cudaMemcpyHostToDevice, c->up));
+  CK(cudaEventRecord(c->st_done[slot], c->up));
+  c->st_head ^= 1;
+  c->st_count += 1;
+  return TL_OK;
+}
+
+int tl_take_staged(tl_ctx* c) {
+  if (!c) return fail(TL_ERR_ARG, "tl_take_staged: null context");
+  if (c->st_count == 0) return fail(TL_ERR_STATE, "tl_take_staged: no state is staged");
+  const int slot = (c->st_head + c->st_count) & 1;  // the oldest
+  CK(cudaStreamWaitEvent(c->stream, c->st_done[slot], 0));
+  const size_t dp = sizeof(double) * c->L.ld, w = sizeof(double) * c->L.nx;
+  CK(cudaMemcpy2DAsync(c->f.density + c->L.at(1, 1), dp, c->xfield(2 * slot) + c->L.at(1, 1), dp, w, c->L.ny,
+                       cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpy2DAsync(c->f.energy1 + c->L.at(1, 1), dp, c->xfield(2 * slot + 1) + c->L.at(1, 1), dp, w, c->L.ny,
+                       cudaMemcpyDeviceToDevice, c->stream));
+  if (c->g.reflective) {
+    int rc = do_halo(c, M(TL_FIELD_DENSITY) | M(TL_FIELD_ENERGY1), c->halo_depth);
+    if (rc) return rc;
+  }
+  CK(cudaEventRecord(c->st_used[slot], c->stream));
+  c->st_used_rec[slot] = true;
+  c->st_count -= 1;
+  return TL_OK;
+}
+
+int tl_fetch_field(tl_ctx* c, int field, double* host, int ld) {
+  if (!c || !host) return fail(TL_ERR_ARG, "tl_fetch_field: null argument");
+  double* d = field_ptr(c, field);
+  if (!d) return fail(TL_ERR_ARG, "tl_fetch_field: unknown field id");
+  if (ld < c->L.nx) return fail(TL_ERR_ARG, "tl_fetch_field: ld < x_cells");
+  int rc;
+  if ((rc = ensure_xfer(c))) return rc;
+  if (c->fe_done_rec) CK(cudaStreamWaitEvent(c->stream, c->fe_done, 0));  // the snapshot is free again
+  CK(cudaMemcpyAsync(c->xfield(4), d, (size_t)c->L.elems() * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaEventRecord(c->fe_snap, c->stream));
+  CK(cudaStreamWaitEvent(c->down, c->fe_snap, 0));
+  CK(cudaMemcpy2DAsync(host, sizeof(double) * ld, c->xfield(4) + c->L.at(1, 1), sizeof(double) * c->L.ld,
+                       sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyDeviceToHost, c->down));
+  CK(cudaEventRecord(c->fe_done, c->down));
+  c->fe_done_rec = true;
+  return TL_OK;
+}
+
+int tl_wait_transfers(tl_ctx* c) {
+  if (!c) return fail(TL_ERR_ARG, "tl_wait_transfers: null context");
+  if (c->up) CK(cudaStreamSynchronize(c->up));
+  if (c->down) CK(cudaStreamSynchronize(c->down));
   return TL_OK;
 }
 

@@ -101,6 +101,10 @@ SIGNATURES = {
     "tl_update_halo": (_I, [_P, _I, _I]),
     "tl_tea_leaf": (_I, [_P, C.POINTER(SolveOpts), _D, C.POINTER(SolveInfo)]),
     "tl_reset_eigen": (_I, [_P]),
+    "tl_stage_state": (_I, [_P, _DP, _DP, _I]),
+    "tl_take_staged": (_I, [_P]),
+    "tl_fetch_field": (_I, [_P, _I, _DP, _I]),
+    "tl_wait_transfers": (_I, [_P]),
     "tl_adjoint_begin": (_I, [_P, _I, _I]),
     "tl_adjoint_record_step": (_I, [_P, C.POINTER(SolveOpts), _D, C.POINTER(SolveInfo)]),
     "tl_adjoint_backward": (_I, [_P, _DP, _DP, _I, _DP, _DP, C.POINTER(SolveInfo)]),
@@ -192,6 +196,7 @@ class Chunk:
         _check(self.L.tl_create(x_cells, y_cells, halo_depth, coefficient, precond, int(bool(reflective)), dx, dy,
                                 C.byref(ptr)))
         self.ptr = ptr
+        self._xfer_refs = []  # host arrays of pipelined transfers in flight
 
     @classmethod
     def from_deck(cls, deck: Deck, generate: bool = True) -> "Chunk":
@@ -238,6 +243,30 @@ class Chunk:
         d = np.ascontiguousarray(density, dtype=np.float64)
         e = np.ascontiguousarray(energy, dtype=np.float64)
         _check(self.L.tl_upload_state(self.ptr, _dp(d), _dp(e), self.nx))
+
+    # ---- pipelined transfers (copies overlapping the solves) ----
+    def stage_state(self, density: np.ndarray, energy: np.ndarray) -> None:
+        """Start copying (density, energy1) into a staging slot; the arrays (page-locked, e.g.
+        PinnedArray) are kept referenced until wait_transfers()."""
+        for a in (density, energy):
+            if a.shape != (self.ny, self.nx) or a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError("expected C-contiguous float64 arrays of shape (y_cells, x_cells)")
+        _check(self.L.tl_stage_state(self.ptr, _dp(density), _dp(energy), self.nx))
+        self._xfer_refs.append((density, energy))
+
+    def take_staged(self) -> None:
+        _check(self.L.tl_take_staged(self.ptr))
+
+    def fetch(self, field: str, out: np.ndarray) -> None:
+        """Start copying a snapshot of a field into out (valid after wait_transfers())."""
+        if out.shape != (self.ny, self.nx) or out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 array of shape (y_cells, x_cells)")
+        _check(self.L.tl_fetch_field(self.ptr, FIELD[field], _dp(out), self.nx))
+        self._xfer_refs.append((out,))
+
+    def wait_transfers(self) -> None:
+        _check(self.L.tl_wait_transfers(self.ptr))
+        self._xfer_refs = []
 
     def device_bytes(self) -> int:
         v = C.c_ulonglong()

@@ -36,7 +36,7 @@ int cuda_fail(cudaError_t e, const char* where) {
 // field order inside the slab
 enum Slot {
   S_DENSITY, S_ENERGY1, S_U, S_U0, S_R, S_W, S_P, S_P2, S_KX, S_KY, S_CX, S_CY, S_DI, S_Z, S_MI, S_SD, S_SD1,
-  S_UTEMP, S_RTEMP, S_RSTORE, S_CP, S_BFP, S_U1, S_JINV, S_COUNT
+  S_UTEMP, S_RTEMP, S_RSTORE, S_CP, S_BFP, S_U1, S_JINV, S_JDEN, S_COUNT
 };
 
 }  // namespace
@@ -109,7 +109,7 @@ struct tl_ctx {
 
   double* slot(int s) const { return reinterpret_cast<double*>(slab + (size_t)s * field_stride); }
   Reduce rd() const { return Reduce{partials, counter, st, hist_a, hist_b, ch_a, ch_b}; }
-  LoopArgs loop() const { return LoopArgs{f, L, rd(), g.precond, g.reflective, g.ry}; }
+  LoopArgs loop() const { return LoopArgs{f, L, rd(), g.precond, g.reflective, g.ry, g.rx}; }
 };
 
 namespace {
@@ -483,6 +483,7 @@ int tl_create(int x_cells, int y_cells, int halo_depth, int coefficient, int pre
   f.bfp = c->slot(S_BFP);
   f.u1 = c->slot(S_U1);
   f.jinv = c->slot(S_JINV);
+  f.jden = c->slot(S_JDEN);
   *out = c;
   return TL_OK;
 }
@@ -890,7 +891,7 @@ int tl_ppcg_calc_rrn(tl_ctx* c, double* rrn) {
 int tl_jacobi_solve(tl_ctx* c, double* error) {
   if (!c || !error) return fail(TL_ERR_ARG, "tl_jacobi_solve: null argument");
   launch_jacobi_denominator(c->f, c->L, c->g, c->stream);
-  launch_jacobi(c->f, c->L, c->rd(), c->stream);
+  launch_jacobi(c->f, c->L, c->g, c->rd(), c->stream);
   int rc = check_launch("jacobi_solve");
   if (rc) return rc;
   return reduce_result(c, error);

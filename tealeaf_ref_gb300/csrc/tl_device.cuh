@@ -30,11 +30,27 @@ struct Layout {
 // solve; kx/ky keep the reference's unscaled values.  p2 is the ping-pong partner of p in
 // the fused CG loop; u1 is the partner of u for kernels that read u's neighbours while
 // producing a new u (Chebyshev, Jacobi); sd1 is the partner of sd for the PPCG inner
-// sweeps; jinv = 1/(Jacobi denominator).
+// sweeps; jden = the Jacobi denominator, jinv = RN(1/jden).
 struct Fields {
   double *density, *energy1, *u, *u0, *r, *w, *p, *p2, *kx, *ky, *cx, *cy, *di, *z, *mi, *sd, *utemp, *rtemp,
-      *r_store, *cp, *bfp, *u1, *sd1, *jinv;
+      *r_store, *cp, *bfp, *u1, *sd1, *jinv, *jden;
 };
+
+// One Jacobi update (tea_leaf_jacobi_kernel.f90:64-68) with the reference's bits: every
+// product and sum in the reference's order, rounded on its own (no contraction), and the
+// quotient num/den correctly rounded from the stored y = RN(1/den) by one remainder
+// correction, q = RN(num y), q + (num - den q) y (P. Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990): three
+// FP64 operations instead of a division.  kx0/kx1 are Kx(j)/Kx(j+1), ky0/ky1 Ky(k)/Ky(k+1).
+__device__ __forceinline__ double jacobi_cell(double u0, double kx0, double kx1, double ky0, double ky1, double ul,
+                                              double ur, double ub, double ut, double den, double y, double rx,
+                                              double ry) {
+  const double sx = __dmul_rn(rx, __dadd_rn(__dmul_rn(kx1, ur), __dmul_rn(kx0, ul)));
+  const double sy = __dmul_rn(ry, __dadd_rn(__dmul_rn(ky1, ut), __dmul_rn(ky0, ub)));
+  const double num = __dadd_rn(__dadd_rn(u0, sx), sy);
+  const double q = __dmul_rn(num, y);
+  return __fma_rn(__fma_rn(-q, den, num), y, q);
+}
 
 // Exit / stop codes written by the device epilogues.
 enum : int {

@@ -582,7 +582,8 @@ struct EpiJacobi {
 // sum |u_out - un|; the epilogue applies the loop's test (error = sqrt|error|) and n = n+1.
 // Off-domain neighbours of un are zero: the reference never writes un's halo.  The same
 // operation order as k_jacobi, so the same bits.
-__global__ void k_fused_jacobi(Fields f, Layout L, Reduce rd, const double* __restrict__ un, double* __restrict__ u_out) {
+__global__ void k_fused_jacobi(Fields f, Layout L, Reduce rd, const double* __restrict__ un, double* __restrict__ u_out,
+                               double rx, double ry) {
   if (rd.st->status != RUN) return;
   double v[1] = {0.0};
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -591,8 +592,8 @@ __global__ void k_fused_jacobi(Fields f, Layout L, Reduce rd, const double* __re
     const long long c = L.at(j, k);
     const double ur = j < L.nx ? un[c + 1] : 0.0, ul = j > 1 ? un[c - 1] : 0.0;
     const double ut = k < L.ny ? un[c + L.ld] : 0.0, ub = k > 1 ? un[c - L.ld] : 0.0;
-    const double num = (f.u0[c] + (f.cx[c + 1] * ur + f.cx[c] * ul)) + (f.cy[c + L.ld] * ut + f.cy[c] * ub);
-    const double u = num * f.jinv[c];
+    const double u = jacobi_cell(f.u0[c], f.kx[c], f.kx[c + 1], f.ky[c], f.ky[c + L.ld], ul, ur, ub, ut, f.jden[c],
+                                 f.jinv[c], rx, ry);
     u_out[c] = u;
     v[0] += fabs(u - un[c]);
   }
@@ -603,7 +604,7 @@ __global__ void k_fused_jacobi(Fields f, Layout L, Reduce rd, const double* __re
 
 void launch_fused_jacobi(const LoopArgs& a, const double* un, double* u_out, cudaStream_t s) {
   const int gy = a.L.ny < 256 ? a.L.ny : 256;
-  { ++launch_counter(); k_fused_jacobi<<<dim3((a.L.nx + 255) / 256, gy), 256, 0, s>>>(a.f, a.L, a.rd, un, u_out); }
+  { ++launch_counter(); k_fused_jacobi<<<dim3((a.L.nx + 255) / 256, gy), 256, 0, s>>>(a.f, a.L, a.rd, un, u_out, a.rx, a.ry); }
 }
 
 void launch_flush_u(const LoopArgs& a, cudaStream_t s) {

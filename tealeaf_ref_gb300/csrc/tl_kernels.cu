@@ -453,28 +453,28 @@ __global__ void k_ppcg_inner_s(Fields f, Layout L, double a, double b, int preco
 
 // tea_leaf_jacobi_solve_kernel (jacobi_kernel.f90:26-77), un = r (copied first); off-domain
 // neighbours of un read its halo, which the reference never writes (zero).
-__global__ void k_jacobi(Fields f, Layout L, Reduce rd) {
+__global__ void k_jacobi(Fields f, Layout L, Reduce rd, double rx, double ry) {
   double v[1] = {0.0};
   FOR_ROWS(L) {
     if (j > L.nx) continue;
     const long long c = L.at(j, k);
     const double* un = f.r;
-    const double num = (f.u0[c] + (f.cx[c + 1] * un[c + 1] + f.cx[c] * un[c - 1])) +
-                       (f.cy[c + L.ld] * un[c + L.ld] + f.cy[c] * un[c - L.ld]);
-    const double u = num * f.jinv[c];
+    const double u = jacobi_cell(f.u0[c], f.kx[c], f.kx[c + 1], f.ky[c], f.ky[c + L.ld], un[c - 1], un[c + 1],
+                                 un[c - L.ld], un[c + L.ld], f.jden[c], f.jinv[c], rx, ry);
     f.u[c] = u;
     v[0] += fabs(u - un[c]);
   }
   grid_reduce<1>(v, rd, EpiMode<1>{rd.st, RED_STORE});
 }
 
-// reciprocal of the Jacobi denominator (jacobi_kernel.f90:67-69), exact operation order
+// the Jacobi denominator (jacobi_kernel.f90:67-69, exact operation order) and its reciprocal
 __global__ void k_jacobi_den(Fields f, Layout L, Geometry g) {
   FOR_ROWS(L) {
     if (j > L.nx) continue;
     const long long c = L.at(j, k);
     const double den = __dadd_rn(__dadd_rn(1.0, __dmul_rn(g.rx, __dadd_rn(f.kx[c], f.kx[c + 1]))),
                                  __dmul_rn(g.ry, __dadd_rn(f.ky[c], f.ky[c + L.ld])));
+    f.jden[c] = den;
     f.jinv[c] = __ddiv_rn(1.0, den);
   }
 }
@@ -593,9 +593,9 @@ void launch_dot(const double* a, const double* b, const double* bminus, const La
                 cudaStream_t s) {
   { ++launch_counter(); k_dot<<<row_grid(L, true), TB, 0, s>>>(a, b, bminus, L, rd, mode); }
 }
-void launch_jacobi(const Fields& f, const Layout& L, const Reduce& rd, cudaStream_t s) {
+void launch_jacobi(const Fields& f, const Layout& L, const Geometry& g, const Reduce& rd, cudaStream_t s) {
   launch_copy_interior(f.r, f.u, L, s);
-  { ++launch_counter(); k_jacobi<<<row_grid(L, true), TB, 0, s>>>(f, L, rd); }
+  { ++launch_counter(); k_jacobi<<<row_grid(L, true), TB, 0, s>>>(f, L, rd, g.rx, g.ry); }
 }
 void launch_jacobi_denominator(const Fields& f, const Layout& L, const Geometry& g, cudaStream_t s) {
   { ++launch_counter(); k_jacobi_den<<<row_grid(L, false), TB, 0, s>>>(f, L, g); }

@@ -60,7 +60,7 @@ void launch_ppcg_init(const Fields& f, const Layout& L, const Geometry& g, int s
 void launch_ppcg_inner(const Fields& f, const Layout& L, const Geometry& g, double a, double b, cudaStream_t s);
 void launch_dot(const double* a, const double* b, const double* bminus /*nullable*/, const Layout& L,
                 const Reduce& rd, int mode, cudaStream_t s);
-void launch_jacobi(const Fields& f, const Layout& L, const Reduce& rd, cudaStream_t s);
+void launch_jacobi(const Fields& f, const Layout& L, const Geometry& g, const Reduce& rd, cudaStream_t s);
 
 // ---- fused solver loop (device-resident scalars) ------------------------
 struct LoopArgs {
@@ -70,6 +70,7 @@ struct LoopArgs {
   int precond;
   int reflective;
   double ry;  // dt/dy^2 (block-Jacobi tridiagonal coefficients)
+  double rx;  // dt/dx^2
 };
 void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s);
 void launch_fused_cg_ur(const LoopArgs& a, bool ppcg, cudaStream_t s);

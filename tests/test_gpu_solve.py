@@ -178,3 +178,21 @@ def test_persistent_cg_barrier_wait_is_bounded(monkeypatch):
         c.generate(d)
         info = c.tea_leaf(d)
         assert info.reported_iterations > 0
+
+
+@pytest.mark.parametrize("reflective", [False, True])
+def test_jacobi_bitwise(reflective):
+    """The device-resident Jacobi loop computes each update with the reference's bits, so
+    after the same number of iterations (tl_eps too small to stop either run) u is
+    bit-for-bit the oracle's, and a solve that reaches an exact fixed point stops at the
+    oracle's iteration."""
+    from oracle import oracle
+    from tealeaf_ref_gb300 import native
+
+    d = small_deck(nx=75, ny=41, steps=2, solver="jacobi", max_iters=400, eps=1e-300, reflective=reflective)
+    o = oracle.Chunk.from_deck(d)
+    want = [o.tea_leaf(d).reported_iterations for _ in range(d.end_step)]
+    with native.Chunk.from_deck(d) as c:
+        got = [c.tea_leaf(d).reported_iterations for _ in range(d.end_step)]
+        np.testing.assert_array_equal(c.download("u"), np.array(o.interior("u")))
+    assert got == want

@@ -248,6 +248,13 @@ bool use_graphs() {
   return !(e && e[0] == '1');
 }
 
+// TL_PPCG_FUSED=0: run the PPCG outer iterations over the per-kernel path (three scalar round
+// trips per iteration) instead of the fused sweeps with device scalars.
+bool use_fused_ppcg() {
+  const char* e = getenv("TL_PPCG_FUSED");
+  return !(e && e[0] == '0');
+}
+
 // The persistent CG kernel replaces the batched kernels up to this many cells (plain or
 // jac_diag preconditioner): per iteration it measured 13.8 / 16.9 / 27.6 / 49.5 us at 128^2 /
 // 256^2 / 512^2 / 1024^2 against 25.6 / 26.2 / 32.3 / 47.6 us for the batched kernels (CUDA
@@ -1204,10 +1211,11 @@ struct Solver {
     return check_launch("mixed chebyshev");
   }
 
-  int run_ppcg_inner_steps(int inner_steps) {
+  // fused: init_sd already ran in the outer update sweep, and z = utemp is left to the rrn sweep
+  int run_ppcg_inner_steps(int inner_steps, bool fused = false) {
     // tea_leaf_ppcg.f90:211-431 on one chunk (every face external: bounds = interior)
     if (inner_steps < 0) return TL_OK;
-    launch_ppcg_init_sd(c->f, c->L, c->g, c->theta, c->stream);
+    if (!fused) launch_ppcg_init_sd(c->f, c->L, c->g, c->theta, c->stream);
     const int h = c->halo_depth;
     int rc;
     for (int cur = 1; cur <= inner_steps; cur += h) {
@@ -1221,8 +1229,50 @@ struct Solver {
         if (step == inner_steps) break;
       }
     }
-    launch_copy_interior(c->f.z, c->f.utemp, c->L, c->stream);
+    if (!fused) launch_copy_interior(c->f.z, c->f.utemp, c->L, c->stream);
     return check_launch("ppcg_inner_steps");
+  }
+
+  // The PPCG outer iterations from the one after the switch set-up to the end of the solve
+  // (tea_solve.f90:289-331), the scalars on the device: the matvec sweep (p = z + beta p,
+  // w = A p, p.w, r_store = r, z.r, alpha), the update sweep (u += alpha p, r -= alpha w,
+  // init_sd), the inner sweeps, and the rrn sweep (z = utemp, (r - r_store).z, beta, the EXIT
+  // test).  One status read per outer iteration instead of three scalar round trips.  p (from
+  // ppcg_init step 3) is in the p field on entry.  Precondition: no preconditioner or jac_diag.
+  int run_fused_ppcg(int n, double rro, double old_error, bool mixed, int inner, int* n_out, double* error,
+                     bool* exited, int* outer_done, int* inner_done) {
+    LoopState& H = *c->st_host;
+    LoopArgs la = c->loop();
+    int rc;
+    // iteration n reads p_{n-1} from (n odd ? p : p2)
+    if (!(n & 1)) launch_copy_all(c->f.p2, c->f.p, c->L, c->stream);
+    H.n = n;
+    H.status = RUN;
+    H.p_pending = 0;
+    H.u_pending = 0;
+    H.check_switch = 0;
+    H.rro = rro;
+    H.old_error = old_error;
+    H.theta = c->theta;
+    if ((rc = push_state(c))) return rc;
+    *outer_done = 0;
+    *inner_done = 0;
+    while (true) {
+      launch_fused_cg_w(la, true, c->stream);
+      launch_fused_ppcg_ur(la, !mixed, c->stream);
+      if ((rc = mixed ? run_ppcg_inner_steps32(inner) : run_ppcg_inner_steps(inner, true))) return rc;
+      launch_fused_ppcg_rrn(la, !mixed, c->stream);
+      if ((rc = check_launch("ppcg outer iteration"))) return rc;
+      if ((rc = sync_state(c))) return rc;
+      *outer_done += 1;
+      *inner_done += inner;
+      if (H.status == EXIT_BREAKDOWN) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite PPCG scalar");
+      if (H.status != RUN) break;
+    }
+    *error = H.error;
+    *exited = H.status == EXIT_CONVERGED;
+    *n_out = *exited ? H.n_exit : H.n;
+    return TL_OK;
   }
 };
 
@@ -1496,6 +1546,13 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
             if ((rc = S.norm(c->f.r, &error))) return rc;
           }
         }
+      } else if (c->g.precond != TL_PREC_JAC_BLOCK && use_fused_ppcg()) {
+        int outer = 0, inner_done = 0;
+        if ((rc = S.run_fused_ppcg(n, rro, old_error, mixed, inner, &n, &error, &exited, &outer, &inner_done)))
+          return rc;
+        ppcg_inner_iters += inner_done;
+        cheby_calc_steps += outer;
+        break;
       } else {
         double pw, rrn;
         launch_cg_calc_w(c->f, c->L, c->rd(), c->stream);

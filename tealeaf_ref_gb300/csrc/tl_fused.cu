@@ -411,12 +411,13 @@ __global__ void __launch_bounds__(FT) k_flush_u(LoopArgs a) {
 //            left pending for the next matvec sweep (LoopState::u_pending);
 //   UR_PPCG  u updated here, no reduction (rrn is discarded, tea_solve.f90:309-311), fused
 //            init_sd of the inner sweeps;
+//   UR_PPCG_NOSD  as UR_PPCG without init_sd (the FP32 inner sweeps start from r themselves);
 //   UR_ONLY  as UR_CG without the reduction: the block-Jacobi solve and r.z follow in
 //            k_fused_block_rz.
-enum { UR_CG = 0, UR_PPCG = 1, UR_ONLY = 2 };
+enum { UR_CG = 0, UR_PPCG = 1, UR_ONLY = 2, UR_PPCG_NOSD = 3 };
 template <int MODE>
 __global__ void __launch_bounds__(FT) k_fused_cg_ur(LoopArgs a) {
-  constexpr bool PPCG = MODE == UR_PPCG;
+  constexpr bool PPCG = MODE == UR_PPCG || MODE == UR_PPCG_NOSD;
   LoopState* st = a.rd.st;
   if (st->status != RUN) return;
   const Layout L = a.L;
@@ -510,6 +511,54 @@ __global__ void __launch_bounds__(FT) k_fused_block_rz(LoopArgs a, double ry) {
   grid_reduce<1>(acc, a.rd, EpiCgUr{a.rd});
 }
 
+// End of a PPCG outer iteration (tea_solve.f90:320-330): z = utemp (tea_leaf_ppcg_update_z,
+// when the FP64 inner sweeps left their result in utemp), rrn = (r - r_store).z
+// (tea_leaf_ppcg_calc_rrn, ppcg_kernel.f90:532-561), and on the device beta = rrn/rro,
+// p pending as z + beta p for the next matvec sweep, rro = rrn, error = rrn and the loop's
+// EXIT test.
+struct EpiPpcgRrn {
+  Reduce rd;
+  __device__ void operator()(double (&acc)[1]) const {
+    LoopState* st = rd.st;
+    const double rrn = acc[0];
+    st->rrn = rrn;
+    st->beta = rrn / st->rro;
+    st->p_pending = 1;
+    st->rro = rrn;
+    finish_iteration(st, rrn);
+  }
+};
+
+template <bool COPY_Z>
+__global__ void __launch_bounds__(FT) k_fused_ppcg_rrn(LoopArgs a) {
+  LoopState* st = a.rd.st;
+  if (st->status != RUN) return;
+  const Layout L = a.L;
+  const int ja = blockIdx.x * SW + 1 + 2 * threadIdx.x;
+  const bool has_b = ja + 1 <= L.nx;
+  double acc[1] = {0.0};
+  if (ja <= L.nx) {
+    for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
+      const long long c = L.at(ja, k);
+      double2 zz;
+      if (COPY_Z) {
+        zz = *reinterpret_cast<const double2*>(a.f.utemp + c);
+        if (has_b)
+          *reinterpret_cast<double2*>(a.f.z + c) = zz;
+        else
+          a.f.z[c] = zz.x;
+      } else {
+        zz = *reinterpret_cast<const double2*>(a.f.z + c);
+      }
+      const double2 rr = *reinterpret_cast<const double2*>(a.f.r + c);
+      const double2 rs = *reinterpret_cast<const double2*>(a.f.r_store + c);
+      acc[0] = fma(rr.x - rs.x, zz.x, acc[0]);
+      if (has_b) acc[0] = fma(rr.y - rs.y, zz.y, acc[0]);
+    }
+  }
+  grid_reduce<1>(acc, a.rd, EpiPpcgRrn{a.rd});
+}
+
 inline int strips(const Layout& L) { return (L.nx + SW - 1) / SW; }
 
 }  // namespace
@@ -550,11 +599,31 @@ cudaError_t launch_persistent_cg(const LoopArgs& a, int max_run, unsigned* bar, 
   return cudaLaunchCooperativeKernel((const void*)k_persistent_cg, dim3(g), dim3(PB_T), args, 0, s);
 }
 
-void launch_fused_cg_ur(const LoopArgs& a, bool ppcg, cudaStream_t s) {
-  const int ns = strips(a.L);
-  int gy = a.L.ny < 512 ? a.L.ny : 512;
+inline dim3 ur_grid(const Layout& L) {
+  const int ns = strips(L);
+  int gy = L.ny < 512 ? L.ny : 512;
   if ((long long)gy * ns > MAX_REDUCE_BLOCKS) gy = MAX_REDUCE_BLOCKS / ns;
-  dim3 grid(ns, gy);
+  return dim3(ns, gy);
+}
+
+void launch_fused_ppcg_ur(const LoopArgs& a, bool init_sd, cudaStream_t s) {
+  const dim3 grid = ur_grid(a.L);
+  if (init_sd)
+    { ++launch_counter(); k_fused_cg_ur<UR_PPCG><<<grid, FT, 0, s>>>(a); }
+  else
+    { ++launch_counter(); k_fused_cg_ur<UR_PPCG_NOSD><<<grid, FT, 0, s>>>(a); }
+}
+
+void launch_fused_ppcg_rrn(const LoopArgs& a, bool copy_z, cudaStream_t s) {
+  const dim3 grid = ur_grid(a.L);
+  if (copy_z)
+    { ++launch_counter(); k_fused_ppcg_rrn<true><<<grid, FT, 0, s>>>(a); }
+  else
+    { ++launch_counter(); k_fused_ppcg_rrn<false><<<grid, FT, 0, s>>>(a); }
+}
+
+void launch_fused_cg_ur(const LoopArgs& a, bool ppcg, cudaStream_t s) {
+  const dim3 grid = ur_grid(a.L);
   if (ppcg) {
     { ++launch_counter(); k_fused_cg_ur<UR_PPCG><<<grid, FT, 0, s>>>(a); }
   } else if (a.precond == 3) {

@@ -74,6 +74,11 @@ struct LoopArgs {
 };
 void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s);
 void launch_fused_cg_ur(const LoopArgs& a, bool ppcg, cudaStream_t s);
+// PPCG outer iteration pieces (with launch_fused_cg_w(a, true, s)): u += alpha p, r -= alpha w
+// (+ init_sd of the FP64 inner sweeps); then z = utemp (copy_z) and rrn = (r - r_store).z with
+// the iteration's epilogue and EXIT test
+void launch_fused_ppcg_ur(const LoopArgs& a, bool init_sd, cudaStream_t s);
+void launch_fused_ppcg_rrn(const LoopArgs& a, bool copy_z, cudaStream_t s);
 // u += alpha p of the last CG iteration when it is still pending (end of a CG phase)
 void launch_flush_u(const LoopArgs& a, cudaStream_t s);
 // persistent cooperative CG (no preconditioner or jac_diag): up to max_run iterations in one

@@ -196,3 +196,35 @@ def test_jacobi_bitwise(reflective):
         got = [c.tea_leaf(d).reported_iterations for _ in range(d.end_step)]
         np.testing.assert_array_equal(c.download("u"), np.array(o.interior("u")))
     assert got == want
+
+
+@pytest.mark.parametrize("case", [dict(), dict(precond="jac_diag"), dict(reflective=True), dict(halo_depth=2),
+                                  dict(precision="mixed"), dict(precision="mixed", reflective=True)],
+                         ids=["none", "jac_diag", "reflective", "halo2", "mixed", "mixed-reflective"])
+def test_fused_ppcg_matches_per_kernel_path(case, monkeypatch):
+    """The PPCG outer iterations with device scalars (fused sweeps, one status read per
+    iteration) against the per-kernel path with host scalars on the same deck: field summary
+    1e-10, u 1e-8, iteration counts within a few (different reduction trees)."""
+    from tealeaf_ref_gb300 import native
+
+    case = dict(case)
+    precision = case.pop("precision", "fp64")
+    kw = dict(nx=203, ny=151, steps=3, n_rect=4, n_circ=2, max_iters=20000, solver="ppcg", ppcg_inner_steps=10,
+              ch_cg_presteps=20)
+    kw.update(case)
+    d = small_deck(**kw)
+    opts = native.opts_from_deck(d, precision=precision)
+    runs = []
+    for fused in ("0", "1"):
+        monkeypatch.setenv("TL_PPCG_FUSED", fused)
+        with native.Chunk.from_deck(d) as c:
+            infos = [c.tea_leaf(opts, d.initial_timestep) for _ in range(d.end_step)]
+            runs.append((c.field_summary(), c.download("u"), infos))
+    (s0, u0, i0), (s1, u1, i1) = runs
+    ok, worst = _summary_close(s1, s0, 1e-10)
+    assert ok, worst
+    assert np.max(np.abs(u1 - u0) / np.abs(u0)) < 1e-8
+    for a, b in zip(i1, i0):
+        assert a.ppcg_inner_iters > 0
+        assert abs(a.reported_iterations - b.reported_iterations) <= max(2, int(0.01 * b.reported_iterations))
+        assert abs(a.ppcg_inner_iters - b.ppcg_inner_iters) <= 10 * max(2, int(0.01 * b.reported_iterations))

@@ -599,9 +599,14 @@ cudaError_t launch_persistent_cg(const LoopArgs& a, int max_run, unsigned* bar, 
   return cudaLaunchCooperativeKernel((const void*)k_persistent_cg, dim3(g), dim3(PB_T), args, 0, s);
 }
 
+// Update sweeps: about 2048 CTAs of 128 threads (13 per SM), each striding over rows.  At
+// 8192^2 the r -= alpha w, r.r sweep took 0.317 ms with 16384 CTAs (512 row groups), 0.270 ms
+// with 4096, 0.262 ms with 2048 and 0.279 ms with 1216: fewer CTAs mean fewer partials for the
+// last CTA to sum and fewer arrivals on the ticket, until too few rows are in flight.
 inline dim3 ur_grid(const Layout& L) {
   const int ns = strips(L);
-  int gy = L.ny < 512 ? L.ny : 512;
+  int gy = (2048 + ns - 1) / ns;
+  if (gy > L.ny) gy = L.ny;
   if ((long long)gy * ns > MAX_REDUCE_BLOCKS) gy = MAX_REDUCE_BLOCKS / ns;
   return dim3(ns, gy);
 }

@@ -451,7 +451,9 @@ void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd,
   if (rows < min_rows) rows = min_rows;
   { ++launch_counter(); k_mix_w<<<dim3(ns, (L.ny + rows - 1) / rows), MT, MIX_W_SMEM, s>>>(m, L, rd, ms, rows); }
   if (between) cudaEventRecord(between, s);
-  int gy = L.ny < 512 ? L.ny : 512;
+  // about 2048 CTAs striding over rows, as the FP64 update sweep (fewer partials to sum)
+  int gy = (2048 + ns - 1) / ns;
+  if (gy > L.ny) gy = L.ny;
   if ((long long)gy * ns > MAX_REDUCE_BLOCKS) gy = MAX_REDUCE_BLOCKS / ns;
   { ++launch_counter(); k_mix_ur<<<dim3(ns, gy), MT, 0, s>>>(m, L, rd, ms); }
 }

@@ -74,6 +74,10 @@ def parse():
                          "4096^2 workloads (Jacobi: 8 rectangles, seed 2, capped at --iters; Chebyshev / PPCG: "
                          "seed 3, 20 CG presteps, PPCG 10 inner steps, solved to tl_eps) and report per-kernel "
                          "GB/s from a separately profiled step")
+    ap.add_argument("--compare-fp64", action="store_true",
+                    help="chebyshev / ppcg with --precision mixed: also solve the first time step from the "
+                         "generated state in both forms and report time, true residual and the mixed form's "
+                         "field-summary and per-cell u differences")
     ap.add_argument("--ch-cg-epslim", type=float, default=None,
                     help="chebyshev / ppcg: override tl_ch_cg_epslim (the error below which CG hands over "
                          "after its presteps; a large value switches right after them)")
@@ -380,6 +384,29 @@ def run_solver(args):
             kernels[name] = {"launches": n, "ms_avg": 1e3 * avg, "bytes_per_cell": basis,
                              "gbs": basis * cells / avg / 1e9}
         c.profile(False)
+    compare = None
+    if args.compare_fp64 and args.precision == "mixed" and args.solver != "jacobi":
+        first = {}
+        for form in ("fp64", "mixed"):
+            o = native.opts_from_deck(d, form)
+            o.check_result = 1
+            with native.Chunk.from_deck(d) as c:
+                i = c.tea_leaf(o, dt)
+                first[form] = (i, c.field_summary(), c.download("u"))
+        (i64, s64, u64), (imx, smx, umx) = first["fp64"], first["mixed"]
+        compare = {
+            "workload": "first time step of the %dx%d workload from its generated state, tl_eps 1e-15" % (cells_n,
+                                                                                                        cells_n),
+            "fp64": {"seconds": i64.solve_seconds, "iterations": i64.reported_iterations,
+                     "relative_true_residual": i64.exact_error / i64.initial_residual},
+            "mixed": {"seconds": imx.solve_seconds, "iterations": imx.reported_iterations,
+                      "cg_presteps": imx.cg_calc_steps,
+                      "relative_true_residual": imx.exact_error / imx.initial_residual,
+                      "stop": native.STOP_REASONS.get(imx.stop_reason, str(imx.stop_reason))},
+            "time_ratio_mixed_over_fp64": imx.solve_seconds / i64.solve_seconds,
+            "field_summary_max_rel_diff": float(max(abs(a - b) / abs(b) for a, b in zip(smx, s64))),
+            "u_max_rel_diff": float((abs(umx - u64) / abs(u64)).max()),
+        }
     peak, peak_kind = measured_peaks()
     for k in kernels.values():
         k["frac_of_peak"] = k["gbs"] / peak
@@ -399,6 +426,7 @@ def run_solver(args):
         "peak_gbs": peak,
         "peak_source": peak_kind,
         "profiled_step_iterations": pinfo.reported_iterations,
+        "mixed_vs_fp64": compare,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic",
         "clocks": clk.summary(),

@@ -248,6 +248,13 @@ bool use_graphs() {
   return !(e && e[0] == '1');
 }
 
+// TL_MIXED_PRESTEPS=0: the precision form of Chebyshev runs its CG presteps in FP64 (as the
+// reference does) instead of as the mixed CG.
+bool use_mixed_presteps() {
+  const char* e = getenv("TL_MIXED_PRESTEPS");
+  return !(e && e[0] == '0');
+}
+
 // TL_PPCG_FUSED=0: run the PPCG outer iterations over the per-kernel path (three scalar round
 // trips per iteration) instead of the fused sweeps with device scalars.
 bool use_fused_ppcg() {
@@ -970,6 +977,8 @@ int sync_mix(tl_ctx* c) {
 // Starts a fresh FP32 CG process on the correction (d must be zero): r = p = u0 - A u.
 int mix_restart(tl_ctx* c, const Reduce& rd, double* floor_est) {
   MixState& H = *c->mst_host;
+  // a fresh direction: the recorded CG process restarts (beta of the previous step = 0)
+  if (H.hist_b && H.n > 1) CK(cudaMemsetAsync(H.hist_b + (H.n - 1), 0, sizeof(double), c->stream));
   launch_mix_trial(c->f, c->mix, c->L, rd, c->mst, true, c->stream);
   int rc;
   if ((rc = check_launch("mixed restart"))) return rc;
@@ -981,13 +990,31 @@ int mix_restart(tl_ctx* c, const Reduce& rd, double* floor_est) {
   return TL_OK;
 }
 
+// The CG presteps of the mixed Chebyshev form, as run by mixed_cg: where they stopped.
+struct MixedPresteps {
+  bool switched = false;     // the switch rule fired (else the CG solve finished the time step)
+  int n = 0;                 // loop index of the first Chebyshev iteration
+  double initial_residual = 0.0, residual = 0.0, floor_est = 0.0;
+  int outer = 0;
+};
+
 // Mixed-precision CG (tl_mixed.cu): FP64 refinement loop around FP32 inner CG solves.
 // Called by tl_tea_leaf after the set-up kernels; finishes the solve (finalise included).
-int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long launches0) {
+// pre (non-null): the CG presteps of the mixed Chebyshev form -- the FP32 steps also stop at
+// the reference's switch rule and record their alpha/beta for the eigenvalue estimate; on a
+// switch the last correction is folded into u and the function returns without finalising.
+int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long launches0,
+             MixedPresteps* pre = nullptr) {
   int rc;
   if ((rc = ensure_mix(c))) return rc;
   MixState& H = *c->mst_host;
   memset(&H, 0, sizeof(H));
+  if (pre) {
+    H.switch_rr = o->ch_cg_epslim * o->ch_cg_epslim;
+    H.presteps = o->ch_cg_presteps;
+    H.hist_a = c->hist_a;
+    H.hist_b = c->hist_b;
+  }
   const double delta = o->inner_tol > 0.0 ? o->inner_tol : 0.5;
   H.delta2 = delta * delta;
   H.max_n = o->max_inner_iters > 0 ? std::min(o->max_inner_iters, o->max_iters) : o->max_iters;
@@ -1052,6 +1079,7 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
       }
     }
     if (H.status == EXIT_BREAKDOWN) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite FP32 CG scalar");
+    const bool switching = pre && H.status == STOP_SWITCH;
     const bool capped = H.n > H.max_n;
     // trial replacement: true FP64 residual of u + d, u itself untouched
     launch_mix_flush_d(c->mix, c->L, c->mst, c->stream);  // the trial's epilogue clears d_pending
@@ -1060,6 +1088,11 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
     if ((rc = sync_mix(c))) return rc;
     const double res_t = std::sqrt(std::fabs(H.trial_rr));
     if (!std::isfinite(res_t)) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite residual");
+    if (switching && !(res_t < prev)) {
+      CK(cudaMemsetAsync(c->mix.d, 0, fbytes, c->stream));  // keep u, drop the correction
+      pre->switched = true;
+      break;
+    }
     if (!(res_t < prev)) {
       // no gain: keep u and drop the correction.  Restart the FP32 process from the true
       // residual of u with a fresh direction; a second failure in a row means u sits at the
@@ -1082,6 +1115,10 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
     stalled = (res_t > 0.9 * prev) ? stalled + 1 : 0;
     if (stalled == 0) stall_restarted = false;
     res = prev = res_t;
+    if (switching) {
+      pre->switched = true;
+      break;
+    }
     if (capped) {
       stop = TL_STOP_CAP;
       break;
@@ -1098,9 +1135,18 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
     }
     // continue the CG process with r replaced by the true residual, search direction kept
     H.beta = H.trial_rr32 / H.rro_prev;
+    if (H.hist_b) CK(cudaMemcpyAsync(H.hist_b + (H.n - 1), &H.beta, sizeof(double), cudaMemcpyHostToDevice, c->stream));
     H.rro = H.rr = H.rr_max = H.trial_rr32;
     H.p_pending = 1;
     H.status = RUN;
+  }
+  if (pre && pre->switched) {
+    pre->n = H.n;
+    pre->initial_residual = initial_residual;
+    pre->residual = res;
+    pre->floor_est = floor_est;
+    pre->outer = outer;
+    return check_launch("mixed CG presteps");
   }
   if (res < o->eps * initial_residual) stop = TL_STOP_EPS;
   const int inner_total = H.n - 1;
@@ -1157,7 +1203,8 @@ struct Solver {
   // error bound fall by 1e-4 (gamma = (sqrt(cn)-1)/(sqrt(cn)+1), as est_itc uses).  Stops at
   // the reference's test on the FP64 residual, at its rounding floor, on a rejected or
   // stalled cycle, or when max_iters steps are used.  Returns the steps taken.
-  int run_mixed_cheby(int budget, double initial_residual, double* error, int* steps, int* stop) {
+  int run_mixed_cheby(int budget, double initial_residual, double* error, int* steps, int* stop,
+                      double* floor_out = nullptr) {
     const Reduce rd = c->rd();
     MixState& H = *c->mst_host;
     const double gamma = (std::sqrt(c->cn) - 1.0) / (std::sqrt(c->cn) + 1.0);
@@ -1208,6 +1255,7 @@ struct Solver {
     }
     *error = res;
     *steps = total;
+    if (floor_out) *floor_out = floor_est;
     return check_launch("mixed chebyshev");
   }
 
@@ -1275,6 +1323,7 @@ struct Solver {
     return TL_OK;
   }
 };
+
 
 }  // namespace
 
@@ -1358,6 +1407,26 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
   bool ch_switch_check = false, ppcg_active = false, exited = false;
   int fields_mask = S.use_jacobi ? M(TL_FIELD_U) : M(TL_FIELD_P);
   const int batch = tl_ctx::BATCH;
+
+  // Precision form without reflective boundaries: the CG presteps before the Chebyshev / PPCG
+  // switch (tea_solve.f90:160-174) run as the mixed CG -- FP32 steps with FP64 residual
+  // replacement, stopping at the reference's switch rule and recording their alpha/beta for
+  // the eigenvalue estimate.  Chebyshev needs them every time step, PPCG only until the
+  // eigenvalues are known.  The switch then proceeds from the FP64 residual of u.
+  const bool mixed_presteps = mixed && !c->g.reflective && use_mixed_presteps() &&
+                              (S.use_cheby || (S.use_ppcg && c->first));
+  int presteps_outer = 0;
+  if (mixed_presteps) {
+    MixedPresteps pre;
+    if ((rc = mixed_cg(c, o, info, launches0, &pre))) return rc;
+    if (!pre.switched) return TL_OK;  // the CG steps finished the time step (finalised)
+    launch_residual(c->f, c->L, nullptr, RED_STORE, c->stream);  // r = u0 - A u in FP64
+    n = pre.n;
+    cg_calc_steps = n - 1;
+    old_error = pre.residual;
+    ch_switch_check = true;
+    presteps_outer = pre.outer;
+  }
 
   while (n <= max_iters) {
     if (!ch_switch_check) {
@@ -1516,11 +1585,30 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
       }
       if (S.use_cheby && mixed) {
         int steps = 0, stop = 0;
-        if ((rc = S.run_mixed_cheby(max_iters - n + 1, initial_residual, &error, &steps, &stop))) return rc;
+        double floor_est = 0.0;
+        if ((rc = S.run_mixed_cheby(max_iters - n + 1, initial_residual, &error, &steps, &stop, &floor_est)))
+          return rc;
+        if (mixed_presteps && (stop == TL_STOP_REJECT || stop == TL_STOP_STALL)) {
+          // cycles that ended rejected or stalled: the mixed CG finishes from u (it stops at
+          // once if u is already at the rounding floor); it finalises and reports
+          const int done = n - 1 + steps;
+          if ((rc = mixed_cg(c, o, info, launches0))) return rc;
+          info->n_exit += done;
+          info->reported_iterations += done;
+          info->cg_calc_steps += cg_calc_steps;
+          info->cheby_calc_steps = steps;
+          info->outer_iterations += presteps_outer;
+          info->initial_residual = initial_residual;
+          info->eigmin = c->eigmin;
+          info->eigmax = c->eigmax;
+          return TL_OK;
+        }
         cheby_calc_steps = steps;
         n += steps;
         info->stop_reason = stop;
         info->true_residual = error;
+        info->residual_floor = floor_est;
+        info->outer_iterations = presteps_outer;
         exited = true;
         break;
       }
@@ -1625,6 +1713,7 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
   info->exact_error = exact_error;
   info->eigmin = c->eigmin;
   info->eigmax = c->eigmax;
+  if (mixed_presteps) info->outer_iterations = presteps_outer;
   info->solve_seconds = ms * 1e-3;
   info->kernel_launches = launch_counter() - launches0;
   return TL_OK;

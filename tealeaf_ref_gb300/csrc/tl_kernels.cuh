@@ -108,6 +108,12 @@ struct MixState {
   double trial_scale;                         // sum of (|u0| + |Di u| + sum |c u_nb|)^2 (last trial)
   double d_alpha;
   int n, max_n, phase_end, status, p_pending, d_pending, d_psel;
+  // CG presteps of the mixed Chebyshev form: stop with STOP_SWITCH once step n >= presteps
+  // and r.r <= switch_rr (the reference's switch rule, tea_solve.f90:167); record alpha/beta
+  // of every step for the eigenvalue estimate (null: not recorded)
+  double switch_rr;
+  int presteps;
+  double *hist_a, *hist_b;
 };
 // once per context (device), before any launch or capture: the FP32 matvec sweep's dynamic
 // shared memory above the 48 KB default; 0 on success

@@ -50,6 +50,10 @@ struct Dot2 {
 
 __device__ __forceinline__ void mix_finish(MixState* ms) {
   ms->n += 1;
+  if (ms->switch_rr > 0.0 && ms->n >= ms->presteps && ms->rr <= ms->switch_rr) {
+    ms->status = STOP_SWITCH;
+    return;
+  }
   // hand over to the host for a residual replacement (the recursive residual fell by delta,
   // or this phase used up its step budget), or stop at the overall cap
   if (!(ms->rr > ms->delta2 * ms->rr_max) || ms->n > ms->max_n || ms->n >= ms->phase_end)
@@ -76,6 +80,7 @@ struct EpiMixW {
     ms->pw = acc[0];
     const double alpha = ms->rro / ms->pw;
     ms->alpha = alpha;
+    if (ms->hist_a) ms->hist_a[ms->n] = alpha;
     if (!isfinite(alpha)) ms->status = EXIT_BREAKDOWN;
   }
 };
@@ -85,6 +90,7 @@ struct EpiMixUr {
   __device__ void operator()(double (&acc)[1]) const {
     ms->rr = acc[0];
     ms->beta = acc[0] / ms->rro;
+    if (ms->hist_b) ms->hist_b[ms->n] = ms->beta;
     ms->rro_prev = ms->rro;
     ms->rro = acc[0];
     ms->p_pending = 1;

@@ -45,6 +45,8 @@ sys.path.insert(0, ROOT)
 # counted because the reference recomputes it from Kx, Ky.
 BYTES_PER_CELL_MATVEC = 64
 BYTES_PER_CELL_IT = 96      # whole FP64 CG iteration (12 streams)
+FP64_OPS_MATVEC = 8         # FP64 operations per cell of the matvec sweep: p update 1, A p 5, p.w 1, deferred u 1
+FP64_OPS_PER_CLOCK_SM = 2   # FP64 pipe peak that ncu reports for GB300: 2 thread-operations per clock per SM
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -604,6 +606,18 @@ def main():
         "iteration_gbs_at_96B": BYTES_PER_CELL_IT * cells * its / dev_s / 1e9 if dev_s else None,
         "note": "FP64 issue rate (measured 0.60 T DFMA/s) bounds the sweep before HBM does",
     }
+    if t_launch:
+        import torch
+
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = clk.summary().get("sm_max_mhz") or 2070.0
+        fp64_peak = FP64_OPS_PER_CLOCK_SM * sms * mhz * 1e6
+        fp64_achieved = FP64_OPS_MATVEC * cells / t_launch
+        roofline["fp64_issue"] = {
+            "ops_per_cell": FP64_OPS_MATVEC, "achieved_tops": fp64_achieved / 1e12, "peak_tops": fp64_peak / 1e12,
+            "frac": fp64_achieved / fp64_peak,
+            "peak_source": "%d FP64 thread-ops per clock per SM (ncu's FP64 pipe peak) x %d SMs x %.0f MHz"
+                           % (FP64_OPS_PER_CLOCK_SM, sms, mhz)}
 
     mixed_cmp = None
     if rank == 0 and world == 1 and not args.no_mixed_compare:

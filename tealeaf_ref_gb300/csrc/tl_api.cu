@@ -464,6 +464,7 @@ int tl_create(int x_cells, int y_cells, int halo_depth, int coefficient, int pre
   if (e == cudaSuccess) e = cudaEventCreate(&c->qe0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->qe1);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) cg_w_slots();  // occupancy of the matvec sweep, queried outside any capture
   if (e != cudaSuccess) {
     int rc = (e == cudaErrorMemoryAllocation) ? TL_ERR_ALLOC : TL_ERR_CUDA;
     g_err = std::string("tl_create: ") + cudaGetErrorString(e);

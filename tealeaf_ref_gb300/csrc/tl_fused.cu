@@ -563,13 +563,39 @@ inline int strips(const Layout& L) { return (L.nx + SW - 1) / SW; }
 
 }  // namespace
 
+int wave_rows(int ny, int ns, long long slots) {
+  if (slots < 1) slots = 1;
+  const long long work = (long long)ny * ns;            // strip-rows to sweep
+  long long waves = (work + slots * 64 - 1) / (slots * 64);  // fewest waves with <= 64 rows per CTA
+  if (waves < 1) waves = 1;
+  long long blocks = waves * slots / ns;                 // row blocks per strip
+  if (blocks < 1) blocks = 1;
+  long long rows = (ny + blocks - 1) / blocks;
+  return (int)(rows < 8 ? 8 : (rows > 64 ? 64 : rows));
+}
+
+long long resident_ctas(const void* kernel, int threads, size_t smem) {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    return 152LL * 8;
+  }
+  return (long long)sms * per_sm;
+}
+
+long long cg_w_slots() {
+  static const long long slots = resident_ctas((const void*)k_fused_cg_w<false>, FT, 0);
+  return slots;
+}
+
 void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s) {
   const int ns = strips(a.L);
-  // 8..64 rows per CTA, aiming at >= ~8 CTAs per SM of 152.  Measured at 8192^2: 64-row
-  // CTAs over three waves (1.031 ms) beat one resident wave of ~196-row CTAs (1.055 ms),
-  // although the latter recomputes fewer edge rows.
-  int rows = (int)(((long long)a.L.ny * ns) / (152 * 8));
-  rows = rows < 8 ? 8 : (rows > 64 ? 64 : rows);
+  // Whole waves of co-resident CTAs, 8..64 rows each.  At 8192^2 that is 64-row CTAs over
+  // three waves (1.031 ms; one resident wave of ~196-row CTAs took 1.055 ms).  At 4096^2 the
+  // earlier rule (8 CTAs per SM) gave 1248 CTAs, 0.91 of a wave.
+  int rows = wave_rows(a.L.ny, ns, cg_w_slots());
   const int min_rows = (int)(((long long)a.L.ny * ns + MAX_REDUCE_BLOCKS - 1) / MAX_REDUCE_BLOCKS);
   if (rows < min_rows) rows = min_rows;  // keep the CTA count within the partials buffer
   dim3 grid(ns, (a.L.ny + rows - 1) / rows);

@@ -72,6 +72,16 @@ struct LoopArgs {
   double ry;  // dt/dy^2 (block-Jacobi tridiagonal coefficients)
   double rx;  // dt/dx^2
 };
+// Rows per CTA of a row-marching sweep over ns strips: whole waves of `slots` co-resident CTAs
+// (SMs x CTAs per SM), 8..64 rows per CTA.
+int wave_rows(int ny, int ns, long long slots);
+// SMs x co-resident CTAs per SM of `kernel` at `threads` threads and `smem` dynamic shared
+// memory (fallback 152 x 8 if the occupancy query fails)
+long long resident_ctas(const void* kernel, int threads, size_t smem);
+// resident CTAs of the FP64 matvec sweep / the FP32 one (queried once; first called outside
+// any stream capture: at context creation / in prepare_mix_kernels)
+long long cg_w_slots();
+long long mix_w_slots();
 void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s);
 void launch_fused_cg_ur(const LoopArgs& a, bool ppcg, cudaStream_t s);
 // PPCG outer iteration pieces (with launch_fused_cg_w(a, true, s)): u += alpha p, r -= alpha w

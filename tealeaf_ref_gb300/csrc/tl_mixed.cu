@@ -444,15 +444,22 @@ void launch_mix_flush_d(const MixFields& m, const Layout& L, MixState* ms, cudaS
   { ++launch_counter(); k_mix_flush_d<<<grid, 256, 0, s>>>(m, L, ms); }
 }
 
+long long mix_w_slots() {
+  static const long long slots = resident_ctas((const void*)k_mix_w, MT, MIX_W_SMEM);
+  return slots;
+}
+
 int prepare_mix_kernels() {
-  return cudaFuncSetAttribute(k_mix_w, cudaFuncAttributeMaxDynamicSharedMemorySize, MIX_W_SMEM) == cudaSuccess ? 0 : -1;
+  if (cudaFuncSetAttribute(k_mix_w, cudaFuncAttributeMaxDynamicSharedMemorySize, MIX_W_SMEM) != cudaSuccess) return -1;
+  mix_w_slots();  // the occupancy query needs the attribute above
+  return 0;
 }
 
 void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd, MixState* ms, cudaStream_t s,
                           cudaEvent_t between) {
   const int ns = mstrips(L);
-  int rows = (int)(((long long)L.ny * ns) / (152 * 8));
-  rows = rows < 8 ? 8 : (rows > 64 ? 64 : rows);
+  // whole waves of co-resident CTAs (three per SM: the staging ring's shared memory)
+  int rows = wave_rows(L.ny, ns, mix_w_slots());
   const int min_rows = (int)(((long long)L.ny * ns + MAX_REDUCE_BLOCKS - 1) / MAX_REDUCE_BLOCKS);
   if (rows < min_rows) rows = min_rows;
   { ++launch_counter(); k_mix_w<<<dim3(ns, (L.ny + rows - 1) / rows), MT, MIX_W_SMEM, s>>>(m, L, rd, ms, rows); }

@@ -228,3 +228,30 @@ def test_fused_ppcg_matches_per_kernel_path(case, monkeypatch):
         assert a.ppcg_inner_iters > 0
         assert abs(a.reported_iterations - b.reported_iterations) <= max(2, int(0.01 * b.reported_iterations))
         assert abs(a.ppcg_inner_iters - b.ppcg_inner_iters) <= 10 * max(2, int(0.01 * b.reported_iterations))
+
+
+def test_two_contexts_interleaved_bitwise():
+    """Two contexts of different shapes alive at once, their solves interleaved (FP64 CG and
+    mixed PPCG): each ends with the bits of the same deck solved alone.  Covers the per-context
+    graphs and state and the process-wide caches (tensor maps, launch shapes)."""
+    from tealeaf_ref_gb300 import native
+
+    da = small_deck(nx=203, ny=151, steps=3, n_rect=4, n_circ=2, max_iters=20000)
+    db = small_deck(nx=301, ny=133, steps=3, n_rect=3, n_circ=1, max_iters=20000, solver="ppcg",
+                    ppcg_inner_steps=10, ch_cg_presteps=20, seed=11)
+    oa = native.opts_from_deck(da)
+    ob = native.opts_from_deck(db, precision="mixed")
+
+    def alone(d, o):
+        with native.Chunk.from_deck(d) as c:
+            for _ in range(d.end_step):
+                c.tea_leaf(o, d.initial_timestep)
+            return c.download("u")
+
+    ua, ub = alone(da, oa), alone(db, ob)
+    with native.Chunk.from_deck(da) as ca, native.Chunk.from_deck(db) as cb:
+        for _ in range(3):
+            ca.tea_leaf(oa, da.initial_timestep)
+            cb.tea_leaf(ob, db.initial_timestep)
+        np.testing.assert_array_equal(ca.download("u"), ua)
+        np.testing.assert_array_equal(cb.download("u"), ub)

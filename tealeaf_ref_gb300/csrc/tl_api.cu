@@ -81,10 +81,16 @@ struct tl_ctx {
   // arguments): the fused CG batch and the mixed-precision CG batch
   cudaGraphExec_t cg_exec = nullptr, mix_exec = nullptr;
   int pgrid = -1;  // co-resident CTAs of the persistent CG kernel (-1: not yet queried)
-  // pipelined host transfers (tl_stage_state, tl_take_staged, tl_fetch_field): an upload and a
-  // download stream, two staging slots of (density, energy1) and one fetch snapshot
+  // host transfers: an upload and a download stream (tl_stage_state, tl_fetch_field) and
+  // XFER_FIELDS staging fields -- two staged (density, energy1) pairs, the fetch snapshot, and
+  // two for the synchronous uploads / downloads.  A host array moves as one contiguous copy
+  // (copy engines) and is unpacked / packed on the device; st_ld[slot] is the host row stride of
+  // a staged pair in that form, 0 for one copied row by row into the context layout.
+  static constexpr int XFER_FIELDS = 7;
   cudaStream_t up = nullptr, down = nullptr;
   char* xfer = nullptr;
+  bool xfer_failed = false;
+  int st_ld[2] = {0, 0};
   cudaEvent_t st_done[2] = {}, st_used[2] = {}, fe_snap = nullptr, fe_done = nullptr;
   bool st_used_rec[2] = {false, false}, fe_done_rec = false;
   int st_head = 0, st_count = 0;
@@ -564,45 +570,6 @@ int tl_device_bytes(const tl_ctx* c, unsigned long long* bytes) {
   return TL_OK;
 }
 
-int tl_upload_field(tl_ctx* c, int field, const double* host, int ld) {
-  if (!c || !host) return fail(TL_ERR_ARG, "tl_upload_field: null argument");
-  double* d = field_ptr(c, field);
-  if (!d) return fail(TL_ERR_ARG, "tl_upload_field: unknown field id");
-  if (ld < c->L.nx) return fail(TL_ERR_ARG, "tl_upload_field: ld < x_cells");
-  CK(cudaMemcpy2DAsync(d + c->L.at(1, 1), sizeof(double) * c->L.ld, host, sizeof(double) * ld,
-                       sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyHostToDevice, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
-  return TL_OK;
-}
-
-int tl_download_field(tl_ctx* c, int field, double* host, int ld) {
-  if (!c || !host) return fail(TL_ERR_ARG, "tl_download_field: null argument");
-  double* d = field_ptr(c, field);
-  if (!d) return fail(TL_ERR_ARG, "tl_download_field: unknown field id");
-  if (ld < c->L.nx) return fail(TL_ERR_ARG, "tl_download_field: ld < x_cells");
-  CK(cudaMemcpy2DAsync(host, sizeof(double) * ld, d + c->L.at(1, 1), sizeof(double) * c->L.ld,
-                       sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
-  return TL_OK;
-}
-
-int tl_upload_state(tl_ctx* c, const double* density, const double* energy1, int ld) {
-  if (!c || !density || !energy1) return fail(TL_ERR_ARG, "tl_upload_state: null argument");
-  if (ld < c->L.nx) return fail(TL_ERR_ARG, "tl_upload_state: ld < x_cells");
-  // Work fields need no clearing: every solve initialises what it reads, and halo cells stay
-  // finite (zero from tl_create, or the generator's / reflective copies).
-  CK(cudaMemcpy2DAsync(c->f.density + c->L.at(1, 1), sizeof(double) * c->L.ld, density, sizeof(double) * ld,
-                       sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyHostToDevice, c->stream));
-  CK(cudaMemcpy2DAsync(c->f.energy1 + c->L.at(1, 1), sizeof(double) * c->L.ld, energy1, sizeof(double) * ld,
-                       sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyHostToDevice, c->stream));
-  if (c->g.reflective) {
-    int rc = do_halo(c, M(TL_FIELD_DENSITY) | M(TL_FIELD_ENERGY1), c->halo_depth);
-    if (rc) return rc;
-  }
-  CK(cudaStreamSynchronize(c->stream));
-  return TL_OK;
-}
-
 }  // extern "C"
 
 namespace {
@@ -616,18 +583,103 @@ int ensure_xfer(tl_ctx* c) {
   }
   CK(cudaEventCreateWithFlags(&c->fe_snap, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&c->fe_done, cudaEventDisableTiming));
-  if (cudaMalloc(&c->xfer, 5 * c->field_stride) != cudaSuccess) {
+  if (cudaMalloc(&c->xfer, tl_ctx::XFER_FIELDS * c->field_stride) != cudaSuccess) {
     cudaGetLastError();
     c->xfer = nullptr;
-    return fail(TL_ERR_ALLOC, "cannot allocate the staging fields of the pipelined transfers");
+    return fail(TL_ERR_ALLOC, "cannot allocate the staging fields of the host transfers");
   }
-  CK(cudaMemsetAsync(c->xfer, 0, 5 * c->field_stride, c->stream));
+  CK(cudaMemsetAsync(c->xfer, 0, tl_ctx::XFER_FIELDS * c->field_stride, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return TL_OK;
+}
+
+// One contiguous copy of a host array of x_cells x y_cells with row stride ld spans this many
+// doubles; it is used when that fits a staging field (always when ld <= the context's stride).
+long long host_span(const Layout& L, int ld) { return (long long)(L.ny - 1) * ld + L.nx; }
+bool span_fits(const tl_ctx* c, int ld) { return host_span(c->L, ld) * (long long)sizeof(double) <= (long long)c->field_stride; }
+
+// the staging fields, allocated on first use; false (and the row-by-row copies) if they cannot be
+bool staging(tl_ctx* c) {
+  if (c->xfer) return true;
+  if (c->xfer_failed) return false;
+  if (ensure_xfer(c) != TL_OK) {
+    c->xfer_failed = true;
+    cudaGetLastError();
+    return false;
+  }
+  return true;
 }
 }  // namespace
 
 extern "C" {
+
+int tl_upload_field(tl_ctx* c, int field, const double* host, int ld) {
+  if (!c || !host) return fail(TL_ERR_ARG, "tl_upload_field: null argument");
+  double* d = field_ptr(c, field);
+  if (!d) return fail(TL_ERR_ARG, "tl_upload_field: unknown field id");
+  if (ld < c->L.nx) return fail(TL_ERR_ARG, "tl_upload_field: ld < x_cells");
+  if (span_fits(c, ld) && staging(c)) {
+    CK(cudaMemcpyAsync(c->xfield(5), host, sizeof(double) * host_span(c->L, ld), cudaMemcpyHostToDevice,
+                       c->stream));
+    launch_unpack(d, c->xfield(5), ld, c->L, c->stream);
+    int rc = check_launch("upload_field");
+    if (rc) return rc;
+  } else {
+    CK(cudaMemcpy2DAsync(d + c->L.at(1, 1), sizeof(double) * c->L.ld, host, sizeof(double) * ld,
+                         sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyHostToDevice, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_download_field(tl_ctx* c, int field, double* host, int ld) {
+  if (!c || !host) return fail(TL_ERR_ARG, "tl_download_field: null argument");
+  double* d = field_ptr(c, field);
+  if (!d) return fail(TL_ERR_ARG, "tl_download_field: unknown field id");
+  if (ld < c->L.nx) return fail(TL_ERR_ARG, "tl_download_field: ld < x_cells");
+  // a dense host array (ld == x_cells) takes one contiguous copy; with ld > x_cells the copy
+  // goes row by row so that the host's columns beyond x_cells are left as they are
+  if (ld == c->L.nx && staging(c)) {
+    launch_pack(c->xfield(5), ld, d, c->L, c->stream);
+    int rc = check_launch("download_field");
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(host, c->xfield(5), sizeof(double) * host_span(c->L, ld), cudaMemcpyDeviceToHost,
+                       c->stream));
+  } else {
+    CK(cudaMemcpy2DAsync(host, sizeof(double) * ld, d + c->L.at(1, 1), sizeof(double) * c->L.ld,
+                         sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
+int tl_upload_state(tl_ctx* c, const double* density, const double* energy1, int ld) {
+  if (!c || !density || !energy1) return fail(TL_ERR_ARG, "tl_upload_state: null argument");
+  if (ld < c->L.nx) return fail(TL_ERR_ARG, "tl_upload_state: ld < x_cells");
+  // Work fields need no clearing: every solve initialises what it reads, and halo cells stay
+  // finite (zero from tl_create, or the generator's / reflective copies).
+  if (span_fits(c, ld) && staging(c)) {
+    const size_t bytes = sizeof(double) * host_span(c->L, ld);
+    CK(cudaMemcpyAsync(c->xfield(5), density, bytes, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->xfield(6), energy1, bytes, cudaMemcpyHostToDevice, c->stream));
+    launch_unpack(c->f.density, c->xfield(5), ld, c->L, c->stream);
+    launch_unpack(c->f.energy1, c->xfield(6), ld, c->L, c->stream);
+    int rc = check_launch("upload_state");
+    if (rc) return rc;
+  } else {
+    CK(cudaMemcpy2DAsync(c->f.density + c->L.at(1, 1), sizeof(double) * c->L.ld, density, sizeof(double) * ld,
+                         sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpy2DAsync(c->f.energy1 + c->L.at(1, 1), sizeof(double) * c->L.ld, energy1, sizeof(double) * ld,
+                         sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyHostToDevice, c->stream));
+  }
+  if (c->g.reflective) {
+    int rc = do_halo(c, M(TL_FIELD_DENSITY) | M(TL_FIELD_ENERGY1), c->halo_depth);
+    if (rc) return rc;
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return TL_OK;
+}
+
 
 int tl_stage_state(tl_ctx* c, const double* density, const double* energy1, int ld) {
   if (!c || !density || !energy1) return fail(TL_ERR_ARG, "tl_stage_state: null argument");
@@ -637,11 +689,20 @@ int tl_stage_state(tl_ctx* c, const double* density, const double* energy1, int 
   if (c->st_count == 2) return fail(TL_ERR_STATE, "tl_stage_state: two states are staged already");
   const int slot = c->st_head;
   if (c->st_used_rec[slot]) CK(cudaStreamWaitEvent(c->up, c->st_used[slot], 0));  // the slot's last take is done
-  const size_t dp = sizeof(double) * c->L.ld, sp = sizeof(double) * ld, w = sizeof(double) * c->L.nx;
-  CK(cudaMemcpy2DAsync(c->xfield(2 * slot) + c->L.at(1, 1), dp, density, sp, w, c->L.ny, cudaMemcpyHostToDevice,
-                       c->up));
-  CK(cudaMemcpy2DAsync(c->xfield(2 * slot + 1) + c->L.at(1, 1), dp, energy1, sp, w, c->L.ny,
-                       cudaMemcpyHostToDevice, c->up));
+  if (span_fits(c, ld)) {
+    // one contiguous copy per array; tl_take_staged unpacks on the device
+    const size_t bytes = sizeof(double) * host_span(c->L, ld);
+    CK(cudaMemcpyAsync(c->xfield(2 * slot), density, bytes, cudaMemcpyHostToDevice, c->up));
+    CK(cudaMemcpyAsync(c->xfield(2 * slot + 1), energy1, bytes, cudaMemcpyHostToDevice, c->up));
+    c->st_ld[slot] = ld;
+  } else {
+    const size_t dp = sizeof(double) * c->L.ld, sp = sizeof(double) * ld, w = sizeof(double) * c->L.nx;
+    CK(cudaMemcpy2DAsync(c->xfield(2 * slot) + c->L.at(1, 1), dp, density, sp, w, c->L.ny,
+                         cudaMemcpyHostToDevice, c->up));
+    CK(cudaMemcpy2DAsync(c->xfield(2 * slot + 1) + c->L.at(1, 1), dp, energy1, sp, w, c->L.ny,
+                         cudaMemcpyHostToDevice, c->up));
+    c->st_ld[slot] = 0;
+  }
   CK(cudaEventRecord(c->st_done[slot], c->up));
   c->st_head ^= 1;
   c->st_count += 1;
@@ -653,11 +714,18 @@ int tl_take_staged(tl_ctx* c) {
   if (c->st_count == 0) return fail(TL_ERR_STATE, "tl_take_staged: no state is staged");
   const int slot = (c->st_head + c->st_count) & 1;  // the oldest
   CK(cudaStreamWaitEvent(c->stream, c->st_done[slot], 0));
-  const size_t dp = sizeof(double) * c->L.ld, w = sizeof(double) * c->L.nx;
-  CK(cudaMemcpy2DAsync(c->f.density + c->L.at(1, 1), dp, c->xfield(2 * slot) + c->L.at(1, 1), dp, w, c->L.ny,
-                       cudaMemcpyDeviceToDevice, c->stream));
-  CK(cudaMemcpy2DAsync(c->f.energy1 + c->L.at(1, 1), dp, c->xfield(2 * slot + 1) + c->L.at(1, 1), dp, w, c->L.ny,
-                       cudaMemcpyDeviceToDevice, c->stream));
+  if (c->st_ld[slot]) {
+    launch_unpack(c->f.density, c->xfield(2 * slot), c->st_ld[slot], c->L, c->stream);
+    launch_unpack(c->f.energy1, c->xfield(2 * slot + 1), c->st_ld[slot], c->L, c->stream);
+    int rc = check_launch("take_staged");
+    if (rc) return rc;
+  } else {
+    const size_t dp = sizeof(double) * c->L.ld, w = sizeof(double) * c->L.nx;
+    CK(cudaMemcpy2DAsync(c->f.density + c->L.at(1, 1), dp, c->xfield(2 * slot) + c->L.at(1, 1), dp, w, c->L.ny,
+                         cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpy2DAsync(c->f.energy1 + c->L.at(1, 1), dp, c->xfield(2 * slot + 1) + c->L.at(1, 1), dp, w,
+                         c->L.ny, cudaMemcpyDeviceToDevice, c->stream));
+  }
   if (c->g.reflective) {
     int rc = do_halo(c, M(TL_FIELD_DENSITY) | M(TL_FIELD_ENERGY1), c->halo_depth);
     if (rc) return rc;
@@ -676,11 +744,22 @@ int tl_fetch_field(tl_ctx* c, int field, double* host, int ld) {
   int rc;
   if ((rc = ensure_xfer(c))) return rc;
   if (c->fe_done_rec) CK(cudaStreamWaitEvent(c->stream, c->fe_done, 0));  // the snapshot is free again
-  CK(cudaMemcpyAsync(c->xfield(4), d, (size_t)c->L.elems() * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  const bool dense = ld == c->L.nx;  // one contiguous copy (else row by row: host columns beyond x_cells kept)
+  if (dense) {
+    launch_pack(c->xfield(4), ld, d, c->L, c->stream);
+    if ((rc = check_launch("fetch_field"))) return rc;
+  } else {
+    CK(cudaMemcpyAsync(c->xfield(4), d, (size_t)c->L.elems() * sizeof(double), cudaMemcpyDeviceToDevice,
+                       c->stream));
+  }
   CK(cudaEventRecord(c->fe_snap, c->stream));
   CK(cudaStreamWaitEvent(c->down, c->fe_snap, 0));
-  CK(cudaMemcpy2DAsync(host, sizeof(double) * ld, c->xfield(4) + c->L.at(1, 1), sizeof(double) * c->L.ld,
-                       sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyDeviceToHost, c->down));
+  if (dense) {
+    CK(cudaMemcpyAsync(host, c->xfield(4), sizeof(double) * host_span(c->L, ld), cudaMemcpyDeviceToHost, c->down));
+  } else {
+    CK(cudaMemcpy2DAsync(host, sizeof(double) * ld, c->xfield(4) + c->L.at(1, 1), sizeof(double) * c->L.ld,
+                         sizeof(double) * c->L.nx, c->L.ny, cudaMemcpyDeviceToHost, c->down));
+  }
   CK(cudaEventRecord(c->fe_done, c->down));
   c->fe_done_rec = true;
   return TL_OK;

@@ -250,6 +250,22 @@ __global__ void k_halo_bt(double* const* fl, int nf, Layout L) {
   }
 }
 
+// The interior of a field (context layout) from / to a host-layout array whose row k starts at
+// (k-1) * ld: the device side of the host transfers, which move the host array with one
+// contiguous copy.
+__global__ void k_unpack(double* __restrict__ dst, const double* __restrict__ src, long long ld, Layout L) {
+  FOR_ROWS(L) {
+    if (j > L.nx) continue;
+    dst[L.at(j, k)] = src[(long long)(k - 1) * ld + (j - 1)];
+  }
+}
+__global__ void k_pack(double* __restrict__ dst, long long ld, const double* __restrict__ src, Layout L) {
+  FOR_ROWS(L) {
+    if (j > L.nx) continue;
+    dst[(long long)(k - 1) * ld + (j - 1)] = src[L.at(j, k)];
+  }
+}
+
 __global__ void k_copy_interior(double* __restrict__ dst, const double* __restrict__ src, Layout L) {
   FOR_ROWS(L) {
     if (j > L.nx) continue;
@@ -513,6 +529,12 @@ void launch_field_summary(const Fields& f, const Layout& L, double cell_vol, con
 void launch_update_halo(double* const* fields, int nfields, const Layout& L, cudaStream_t s) {
   { ++launch_counter(); k_halo_lr<<<(L.ny + 2 + TB - 1) / TB, TB, 0, s>>>(fields, nfields, L); }
   { ++launch_counter(); k_halo_bt<<<(L.nx + 2 + TB - 1) / TB, TB, 0, s>>>(fields, nfields, L); }
+}
+void launch_unpack(double* dst, const double* src, long long ld, const Layout& L, cudaStream_t s) {
+  { ++launch_counter(); k_unpack<<<row_grid(L, false), TB, 0, s>>>(dst, src, ld, L); }
+}
+void launch_pack(double* dst, long long ld, const double* src, const Layout& L, cudaStream_t s) {
+  { ++launch_counter(); k_pack<<<row_grid(L, false), TB, 0, s>>>(dst, ld, src, L); }
 }
 void launch_copy_interior(double* dst, const double* src, const Layout& L, cudaStream_t s) {
   { ++launch_counter(); k_copy_interior<<<row_grid(L, false), TB, 0, s>>>(dst, src, L); }

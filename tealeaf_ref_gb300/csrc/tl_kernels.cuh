@@ -32,6 +32,9 @@ void launch_generate(const Fields& f, const Layout& L, int nstates, const double
 void launch_field_summary(const Fields& f, const Layout& L, double cell_vol, const Reduce& rd, cudaStream_t s);
 void launch_update_halo(double* const* fields, int nfields, const Layout& L, cudaStream_t s);
 void launch_copy_interior(double* dst, const double* src, const Layout& L, cudaStream_t s);
+// interior of a field <- / -> a host-layout array (row k at (k-1)*ld) already on the device
+void launch_unpack(double* dst, const double* src, long long ld, const Layout& L, cudaStream_t s);
+void launch_pack(double* dst, long long ld, const double* src, const Layout& L, cudaStream_t s);
 void launch_copy_all(double* dst, const double* src, const Layout& L, cudaStream_t s);
 
 // ---- per-kernel entry points (reference semantics) ----------------------

@@ -94,3 +94,45 @@ def test_fetch_snapshot_is_taken_in_stream_order():
         c.wait_transfers()
         np.testing.assert_array_equal(out, first)
         assert not np.array_equal(c.download("u"), first)
+
+
+@pytest.mark.parametrize("pad", [4, 70], ids=["contiguous", "row-by-row"])
+def test_host_row_stride(pad):
+    """Host arrays with a row stride ld > x_cells (a Fortran array with halo columns): the
+    interior moves in both directions and the host's extra columns are left untouched.  ld =
+    x_cells + 4 moves as one contiguous copy; x_cells + 70 exceeds the context's stride and goes
+    row by row."""
+    import ctypes as C
+
+    from tealeaf_ref_gb300 import native
+
+    d = small_deck(nx=37, ny=23, steps=1, n_rect=2, n_circ=1)
+    nx, ny, ld = d.x_cells, d.y_cells, d.x_cells + pad
+    rng = np.random.default_rng(5)
+    rho = rng.random((ny, nx)) + 0.5
+    e = rng.random((ny, nx)) + 1.0
+    big_rho = np.full((ny, ld), -7.0)
+    big_e = np.full((ny, ld), -7.0)
+    big_rho[:, :nx] = rho
+    big_e[:, :nx] = e
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    with native.Chunk.from_deck(d) as c:
+        L = c.L
+        assert L.tl_upload_state(c.ptr, dp(big_rho), dp(big_e), ld) == 0
+        np.testing.assert_array_equal(c.download("density"), rho)
+        np.testing.assert_array_equal(c.download("energy1"), e)
+        out = np.full((ny, ld), 3.5)
+        assert L.tl_download_field(c.ptr, native.FIELD["density"], dp(out), ld) == 0
+        np.testing.assert_array_equal(out[:, :nx], rho)
+        assert np.all(out[:, nx:] == 3.5)
+        assert L.tl_upload_field(c.ptr, native.FIELD["u"], dp(big_e), ld) == 0
+        np.testing.assert_array_equal(c.download("u"), e)
+        # pipelined forms
+        assert L.tl_stage_state(c.ptr, dp(big_e), dp(big_rho), ld) == 0
+        assert L.tl_take_staged(c.ptr) == 0
+        out2 = np.full((ny, ld), 4.5)
+        assert L.tl_fetch_field(c.ptr, native.FIELD["density"], dp(out2), ld) == 0
+        assert L.tl_wait_transfers(c.ptr) == 0
+        np.testing.assert_array_equal(out2[:, :nx], e)
+        assert np.all(out2[:, nx:] == 4.5)
+        np.testing.assert_array_equal(c.download("energy1"), rho)

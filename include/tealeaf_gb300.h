@@ -153,7 +153,8 @@ const char* tl_last_error(void);
 /* Make `device` the calling thread's current CUDA device for later tl_create calls (one
  * process per GPU; the reference's one-MPI-rank-per-chunk layout, tea.f90:43-76). */
 int tl_set_device(int device);
-/* Total device bytes the context holds. */
+/* Total device bytes the context holds: the field slab and scratch, plus the buffers made on
+ * first use (FP32 fields of the precision form, adjoint checkpoints, transfer staging). */
 int tl_device_bytes(const tl_ctx* ctx, unsigned long long* bytes);
 
 /* Page-lock (register) an existing host array so that uploads/downloads run at full link

@@ -102,6 +102,7 @@ struct tl_ctx {
   long long nlaunch = 0;  // kernels launched by the current tl_tea_leaf call
   // mixed-precision form: FP32 fields (allocated on first use) and the inner-loop state
   char* mix_slab = nullptr;
+  size_t mix_bytes = 0, tape_bytes = 0;  // sizes of the FP32 slab and the adjoint tape (0: none)
   MixFields mix{};
   MixState* mst = nullptr;
   MixState* mst_host = nullptr;
@@ -566,7 +567,8 @@ int tl_host_unregister(void* host) {
 int tl_device_bytes(const tl_ctx* c, unsigned long long* bytes) {
   if (!c || !bytes) return fail(TL_ERR_ARG, "tl_device_bytes: null argument");
   *bytes = c->slab_bytes + sizeof(double) * 4 * MAX_REDUCE_BLOCKS + 256 + sizeof(LoopState) +
-           sizeof(double) * 2 * ((size_t)c->hist_cap + c->ch_cap);
+           sizeof(double) * 2 * ((size_t)c->hist_cap + c->ch_cap) + c->mix_bytes + (c->tape ? c->tape_bytes : 0) +
+           (c->xfer ? (size_t)tl_ctx::XFER_FIELDS * c->field_stride : 0);
   return TL_OK;
 }
 
@@ -1037,6 +1039,7 @@ int ensure_mix(tl_ctx* c) {
   if (c->mix_slab) return TL_OK;
   const size_t fb = ((size_t)c->L.elems() * sizeof(float) + 4 * 256 + 255) / 256 * 256;
   CK(cudaMalloc(&c->mix_slab, fb * 9));
+  c->mix_bytes = fb * 9;
   CK(cudaMemsetAsync(c->mix_slab, 0, fb * 9, c->stream));
   float* b = reinterpret_cast<float*>(c->mix_slab);
   const size_t step = fb / sizeof(float);
@@ -1826,6 +1829,7 @@ extern "C" int tl_adjoint_begin(tl_ctx* c, int max_steps, int store_solutions) {
     return fail(TL_ERR_ALLOC, "tl_adjoint_begin: cannot allocate the checkpoint fields");
   }
   CK(cudaMemsetAsync(c->tape, 0, nf * c->field_stride, c->stream));
+  c->tape_bytes = nf * c->field_stride;
   c->tape_max = max_steps;
   c->tape_store_u = store_solutions;
   c->tape_dt.assign(max_steps, 0.0);

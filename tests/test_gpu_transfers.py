@@ -136,3 +136,19 @@ def test_host_row_stride(pad):
         np.testing.assert_array_equal(out2[:, :nx], e)
         assert np.all(out2[:, nx:] == 4.5)
         np.testing.assert_array_equal(c.download("energy1"), rho)
+
+
+def test_device_bytes_counts_buffers_made_on_first_use():
+    """tl_device_bytes grows when the precision form's FP32 fields and the transfer staging
+    fields are first made."""
+    from tealeaf_ref_gb300 import native
+
+    d = small_deck(nx=64, ny=48, steps=1, n_rect=2, n_circ=1)
+    with native.Chunk.from_deck(d) as c:
+        b0 = c.device_bytes()
+        assert b0 > 25 * 8 * (48 + 2) * 64  # the field slab at least
+        c.tea_leaf(native.opts_from_deck(d, precision="mixed"), d.initial_timestep)
+        b1 = c.device_bytes()
+        assert b1 > b0
+        c.download("u")  # the staging fields of the host transfers
+        assert c.device_bytes() > b1

@@ -269,6 +269,16 @@ int tl_tea_leaf(tl_ctx* ctx, const tl_solve_opts* opts, double dt, tl_solve_info
 /* Forget the saved eigenvalue estimates (the reference's 'first' flag becomes true). */
 int tl_reset_eigen(tl_ctx* ctx);
 
+/* Host math of the CG -> Chebyshev / PPCG switch, as tl_tea_leaf runs it (no device work, no
+ * context).  tl_cg_eigenvalues: extreme eigenvalues of the Lanczos tridiagonal built from
+ * cg_alphas(1..nsteps), cg_betas(1..nsteps) (tea_leaf_cheby.f90:142-176), by Sturm-sequence
+ * bisection; unscaled (the solve then takes 0.95 eigmin, 1.05 eigmax); TL_ERR_EIGEN when the
+ * estimate is negative or not finite (tea_solve.f90:192).  tl_cheby_coefficients: theta and
+ * the Chebyshev coefficients ch_alphas(1..n), ch_betas(1..n) (tea_leaf_cheby.f90:178-205),
+ * written to [0, n). */
+int tl_cg_eigenvalues(const double* cg_alphas, const double* cg_betas, int nsteps, double* eigmin, double* eigmax);
+int tl_cheby_coefficients(double eigmin, double eigmax, int n, double* ch_alphas, double* ch_betas, double* theta);
+
 /* ---- adjoint (no counterpart in the reference) --------------------------- */
 
 /* Reverse mode of a run of tea_leaf() time steps: gradients of a loss on the final u (and/or

@@ -1009,6 +1009,26 @@ int tl_reset_eigen(tl_ctx* c) {
   return TL_OK;
 }
 
+int tl_cg_eigenvalues(const double* cg_alphas, const double* cg_betas, int nsteps, double* eigmin, double* eigmax) {
+  if (!cg_alphas || !cg_betas || !eigmin || !eigmax || nsteps < 1)
+    return fail(TL_ERR_ARG, "tl_cg_eigenvalues: null argument or nsteps < 1");
+  const std::vector<double> a(cg_alphas, cg_alphas + nsteps), b(cg_betas, cg_betas + nsteps);
+  if (calc_eigenvalues(a, b, nsteps, eigmin, eigmax)) return fail(TL_ERR_EIGEN, "Error in calculating eigenvalues");
+  return TL_OK;
+}
+
+int tl_cheby_coefficients(double eigmin, double eigmax, int n, double* ch_alphas, double* ch_betas, double* theta) {
+  if (!ch_alphas || !ch_betas || !theta || n < 1) return fail(TL_ERR_ARG, "tl_cheby_coefficients: null argument or n < 1");
+  if (!(eigmax > eigmin)) return fail(TL_ERR_ARG, "tl_cheby_coefficients: eigmax must exceed eigmin");
+  std::vector<double> a, b;
+  calc_ch_coefs(a, b, eigmin, eigmax, theta, n);
+  for (int i = 1; i <= n; ++i) {
+    ch_alphas[i - 1] = a[i];
+    ch_betas[i - 1] = b[i];
+  }
+  return TL_OK;
+}
+
 int tl_profile(tl_ctx* c, int enable) {
   if (!c) return fail(TL_ERR_ARG, "tl_profile: null context");
   c->prof = enable != 0;

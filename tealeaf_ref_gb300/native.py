@@ -101,6 +101,8 @@ SIGNATURES = {
     "tl_update_halo": (_I, [_P, _I, _I]),
     "tl_tea_leaf": (_I, [_P, C.POINTER(SolveOpts), _D, C.POINTER(SolveInfo)]),
     "tl_reset_eigen": (_I, [_P]),
+    "tl_cg_eigenvalues": (_I, [_DP, _DP, _I, _DP, _DP]),
+    "tl_cheby_coefficients": (_I, [_D, _D, _I, _DP, _DP, _DP]),
     "tl_stage_state": (_I, [_P, _DP, _DP, _I]),
     "tl_take_staged": (_I, [_P]),
     "tl_fetch_field": (_I, [_P, _I, _DP, _I]),
@@ -176,12 +178,31 @@ def _dp(a: np.ndarray):
 
 def opts_from_deck(deck: Deck, precision: str = "fp64", inner_tol: float = 0.0,
                    max_inner_iters: int = 0) -> SolveOpts:
-    """Solve options from a deck; ``precision`` "mixed" selects FP32 inner CG solves inside
-    FP64 iterative refinement (CG without preconditioner)."""
+    """Solve options from a deck; ``precision`` "mixed" selects the precision form (FP32 sweeps
+    inside FP64 refinement; CG, Chebyshev and PPCG without preconditioner)."""
     return SolveOpts(solver=deck.solver_id, max_iters=deck.max_iters, eps=deck.eps, ch_cg_presteps=deck.ch_cg_presteps,
                      ch_cg_epslim=deck.ch_cg_epslim, ppcg_inner_steps=deck.effective_inner_steps(),
                      check_result=int(deck.check_result), precision=PRECISION[precision], inner_tol=inner_tol,
                      max_inner_iters=max_inner_iters)
+
+
+def cg_eigenvalues(alphas: np.ndarray, betas: np.ndarray) -> tuple:
+    """Extreme eigenvalues of the Lanczos tridiagonal of CG coefficients alphas(1..n), betas(1..n)
+    (tl_cg_eigenvalues; host math, no GPU), unscaled."""
+    a = np.ascontiguousarray(alphas, dtype=np.float64)
+    b = np.ascontiguousarray(betas, dtype=np.float64)
+    if a.shape != b.shape or a.ndim != 1:
+        raise ValueError("alphas and betas must be 1-D arrays of the same length")
+    lo, hi = C.c_double(), C.c_double()
+    _check(load().tl_cg_eigenvalues(_dp(a), _dp(b), a.size, C.byref(lo), C.byref(hi)))
+    return lo.value, hi.value
+
+
+def cheby_coefficients(eigmin: float, eigmax: float, n: int) -> tuple:
+    """(theta, ch_alphas(1..n), ch_betas(1..n)) of the Chebyshev iteration (tl_cheby_coefficients)."""
+    a, b, th = np.zeros(n), np.zeros(n), C.c_double()
+    _check(load().tl_cheby_coefficients(eigmin, eigmax, n, _dp(a), _dp(b), C.byref(th)))
+    return th.value, a, b
 
 
 class Chunk:

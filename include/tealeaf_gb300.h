@@ -162,7 +162,10 @@ int tl_device_bytes(const tl_ctx* ctx, unsigned long long* bytes);
 int tl_host_register(void* host, unsigned long long bytes);
 int tl_host_unregister(void* host);
 
-/* Host <-> device copies of one field's interior (x_cells x y_cells, leading dimension ld). */
+/* Host <-> device copies of one field's interior (x_cells x y_cells, leading dimension ld).
+ * The host array moves as one contiguous copy and is unpacked / packed on the device (the
+ * first call allocates the staging fields); a download with ld > x_cells copies row by row so
+ * that the host columns beyond x_cells are not written. */
 int tl_upload_field(tl_ctx* ctx, int field, const double* host, int ld);
 int tl_download_field(tl_ctx* ctx, int field, double* host, int ld);
 /* Set density and energy1 from host arrays (the state after start.f90:113-123 for a chunk

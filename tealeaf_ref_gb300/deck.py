@@ -78,6 +78,10 @@ class Deck:
     profiler_on: bool = False
     verbose_on: bool = False
     tiles_per_task: int = 1
+    # read and kept for the record; a GPU chunk is one tile (read_input.f90:175-184, 221)
+    sub_tiles_per_tile: int = 1
+    tiles_per_problem: int = 0
+    use_fortran_kernels: bool = True
 
     @property
     def solver_id(self) -> int:
@@ -196,7 +200,8 @@ def parse_deck(text: str) -> Deck:
                 d.end_step = int(nxt)
             elif w in ("xmin", "xmax", "ymin", "ymax"):
                 setattr(d, w, _rval(nxt))
-            elif w in ("x_cells", "y_cells", "visit_frequency", "summary_frequency", "tiles_per_task"):
+            elif w in ("x_cells", "y_cells", "visit_frequency", "summary_frequency", "tiles_per_task",
+                       "sub_tiles_per_tile", "tiles_per_problem"):
                 setattr(d, w, int(nxt))
             elif w == "tl_ch_cg_presteps":
                 d.ch_cg_presteps = int(nxt)
@@ -236,6 +241,8 @@ def parse_deck(text: str) -> Deck:
                     d.profiler_on = True
                 elif w == "verbose_on":
                     d.verbose_on = True
+                elif w == "use_fortran_kernels":
+                    d.use_fortran_kernels = True
                 elif w == "tl_coefficient_density":
                     d.coefficient = CONDUCTIVITY
                 elif w == "tl_coefficient_inverse_density":

@@ -72,3 +72,13 @@ def test_splitmix64_known_values():
     # SplitMix64 with seed 0: first output is 0xE220A8397B1DCDAF (published test vector)
     g = dk.SplitMix64(0)
     assert g.next_u64() == 0xE220A8397B1DCDAF
+
+
+def test_tiling_keywords_are_read():
+    """The tiling keywords take a value (read_input.f90:175-184) and must not leave it behind
+    as a stray word; use_fortran_kernels is a flag."""
+    text = ("*tea\nstate 1 density=100.0 energy=0.0001\nx_cells 10\ny_cells 12\ntiles_per_problem 4\n"
+            "sub_tiles_per_tile 2\nuse_fortran_kernels\ntl_max_iters 77\n*endtea\n")
+    d = dk.parse_deck(text)
+    assert (d.tiles_per_problem, d.sub_tiles_per_tile, d.use_fortran_kernels) == (4, 2, True)
+    assert (d.x_cells, d.y_cells, d.max_iters) == (10, 12, 77)

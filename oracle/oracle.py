@@ -29,10 +29,9 @@ _libs = {}
 
 
 def build(force: bool = False) -> None:
-    """Compile the oracle libraries with oracle/Makefile."""
-    need = force or not all(os.path.exists(os.path.join(BUILD, n)) for n in ("liboracle.so", "liboracle_omp.so"))
-    if need:
-        subprocess.run(["make", "-s", "-C", HERE] + (["-B"] if force else []), check=True)
+    """Compile the oracle libraries with oracle/Makefile (make rebuilds what is stale: the
+    sources or the recipe changed)."""
+    subprocess.run(["make", "-s", "-C", HERE] + (["-B"] if force else []), check=True)
 
 
 class _Opts(C.Structure):

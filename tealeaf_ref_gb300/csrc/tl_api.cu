@@ -577,14 +577,15 @@ int tl_device_bytes(const tl_ctx* c, unsigned long long* bytes) {
 namespace {
 int ensure_xfer(tl_ctx* c) {
   if (c->xfer) return TL_OK;
-  CK(cudaStreamCreateWithFlags(&c->up, cudaStreamNonBlocking));
-  CK(cudaStreamCreateWithFlags(&c->down, cudaStreamNonBlocking));
+  // each handle is made once, so a retry after a failed allocation leaks nothing
+  if (!c->up) CK(cudaStreamCreateWithFlags(&c->up, cudaStreamNonBlocking));
+  if (!c->down) CK(cudaStreamCreateWithFlags(&c->down, cudaStreamNonBlocking));
   for (int i = 0; i < 2; ++i) {
-    CK(cudaEventCreateWithFlags(&c->st_done[i], cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&c->st_used[i], cudaEventDisableTiming));
+    if (!c->st_done[i]) CK(cudaEventCreateWithFlags(&c->st_done[i], cudaEventDisableTiming));
+    if (!c->st_used[i]) CK(cudaEventCreateWithFlags(&c->st_used[i], cudaEventDisableTiming));
   }
-  CK(cudaEventCreateWithFlags(&c->fe_snap, cudaEventDisableTiming));
-  CK(cudaEventCreateWithFlags(&c->fe_done, cudaEventDisableTiming));
+  if (!c->fe_snap) CK(cudaEventCreateWithFlags(&c->fe_snap, cudaEventDisableTiming));
+  if (!c->fe_done) CK(cudaEventCreateWithFlags(&c->fe_done, cudaEventDisableTiming));
   if (cudaMalloc(&c->xfer, tl_ctx::XFER_FIELDS * c->field_stride) != cudaSuccess) {
     cudaGetLastError();
     c->xfer = nullptr;

@@ -1649,7 +1649,9 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
       break;
     }
 
-    // ---- Chebyshev / PPCG iteration n (host-driven over the per-kernel path) ----
+    // ---- Chebyshev / PPCG from iteration n: the switch set-up over the per-kernel path, then
+    // Chebyshev iterations launched one by one, or the PPCG outer iterations as fused sweeps
+    // (run_fused_ppcg; the per-kernel path for jac_block or TL_PPCG_FUSED=0) ----
     if ((S.use_cheby || S.use_ppcg) && ch_switch_check) {
       if (cheby_calc_steps == 0) {
         max_cheby_iters = max_iters - n + 2;

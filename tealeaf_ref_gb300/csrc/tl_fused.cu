@@ -9,6 +9,12 @@
 // p_{n-1} and p_n live in two buffers (P[(n-1)&1] -> P[n&1]) so that the CTA computing a
 // halo row of p_n never sees a neighbour's already-updated value.
 //
+// FP64 PPCG outer iteration (tea_solve.f90:289-331): k_fused_cg_w<PPCG> (p = z + beta p,
+// w = A p, p.w, r_store = r, z.r, alpha), k_fused_cg_ur in a PPCG mode (u, r updates, init_sd),
+// the inner sweeps, then k_fused_ppcg_rrn (z = utemp, (r - r_store).z, beta, the EXIT test).
+// Also here: the persistent cooperative CG kernel for small meshes and the device-resident
+// Jacobi sweep.
+//
 // The matvec kernel marches up a strip of 2*FT columns, one row per step: each thread owns
 // two adjacent columns (16-byte loads), keeps p of rows k-1, k, k+1 in registers and swaps
 // row k through shared memory for the horizontal neighbours; the two strip-edge columns

@@ -291,7 +291,7 @@ int run_cg_batch(tl_ctx* c, const LoopArgs& la) {
     int rc = capture_batch(c, &c->cg_exec, &c->cg_nk, [&] {
       for (int i = 0; i < tl_ctx::BATCH; ++i) {
         launch_fused_cg_w(la, false, c->stream);
-        launch_fused_cg_ur(la, false, c->stream);
+        launch_fused_cg_ur(la, c->stream);
       }
     });
     if (rc) return rc;
@@ -1563,7 +1563,7 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
           if (c->prof) CK(cudaEventRecord(c->pev[3 * i], c->stream));
           launch_fused_cg_w(la, false, c->stream);
           if (c->prof) CK(cudaEventRecord(c->pev[3 * i + 1], c->stream));
-          launch_fused_cg_ur(la, false, c->stream);
+          launch_fused_cg_ur(la, c->stream);
           if (c->prof) CK(cudaEventRecord(c->pev[3 * i + 2], c->stream));
         }
       }

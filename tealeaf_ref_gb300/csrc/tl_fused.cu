@@ -659,11 +659,9 @@ void launch_fused_ppcg_rrn(const LoopArgs& a, bool copy_z, cudaStream_t s) {
     { ++launch_counter(); k_fused_ppcg_rrn<false><<<grid, FT, 0, s>>>(a); }
 }
 
-void launch_fused_cg_ur(const LoopArgs& a, bool ppcg, cudaStream_t s) {
+void launch_fused_cg_ur(const LoopArgs& a, cudaStream_t s) {
   const dim3 grid = ur_grid(a.L);
-  if (ppcg) {
-    { ++launch_counter(); k_fused_cg_ur<UR_PPCG><<<grid, FT, 0, s>>>(a); }
-  } else if (a.precond == 3) {
+  if (a.precond == 3) {
     { ++launch_counter(); k_fused_cg_ur<UR_ONLY><<<grid, FT, 0, s>>>(a); }
     const int gx = (a.L.nx + FT - 1) / FT;
     int by = (a.L.ny + 3) / 4;

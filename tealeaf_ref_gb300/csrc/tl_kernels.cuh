@@ -86,7 +86,7 @@ long long resident_ctas(const void* kernel, int threads, size_t smem);
 long long cg_w_slots();
 long long mix_w_slots();
 void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s);
-void launch_fused_cg_ur(const LoopArgs& a, bool ppcg, cudaStream_t s);
+void launch_fused_cg_ur(const LoopArgs& a, cudaStream_t s);
 // PPCG outer iteration pieces (with launch_fused_cg_w(a, true, s)): u += alpha p, r -= alpha w
 // (+ init_sd of the FP64 inner sweeps); then z = utemp (copy_z) and rrn = (r - r_store).z with
 // the iteration's epilogue and EXIT test

@@ -1,30 +1,41 @@
 #!/usr/bin/env python3
-"""Benchmark: FP64 CG cell-iterations/s of TeaLeaf's implicit solve at 8192^2 on GB300.
+"""Benchmark of TeaLeaf's implicit solve (tea_leaf(), tea_solve.f90:37-503) on GB300.
 
-Workload (synthetic config 5): 8192 x 8192 cells on the 10 x 10 domain, ambient state
-(density 100, energy 1e-4) + 16 seeded rectangles (density U[0.1,1], energy U[1,25]) +
-4 seeded circles (density 0.1, energy 25), reciprocal-density coefficient keyword,
-dt 0.004, tl_eps 1e-15, CG, FP64.  A step is one tea_leaf() time-step solve through the
-C ABI capped at --iters CG iterations (tl_max_iters, default 500): Kx/Ky/Di set-up, initial
-residual, --iters fused CG iterations, finalise.  At this size a full time step needs tens
-of thousands of iterations, so the cap keeps a step under a second; iterations are the work
-unit of the metric (cells x iterations / time), as in the reference's own grind figures.
+Default line (the headline): FP64 CG cell-iterations/s at 8192^2.  Workload: 8192 x 8192
+cells on the 10 x 10 domain, ambient state (density 100, energy 1e-4) + 16 seeded rectangles
+(density U[0.1,1], energy U[1,25]) + 4 seeded circles (density 0.1, energy 25),
+reciprocal-density coefficient keyword, dt 0.004, tl_eps 1e-15, CG, FP64.  A step is one
+tea_leaf() time-step solve through the C ABI capped at --iters CG iterations (tl_max_iters,
+default 500): set-up, initial residual, the fused CG iterations, finalise.  At this size a full
+time step needs tens of thousands of iterations, so the cap keeps a step under a second;
+iterations are the work unit of the metric (cells x iterations / time), as in the reference's
+own grind figures.
+
+--solver jacobi | chebyshev | ppcg: the same line for the 4096^2 workloads (8 seeded
+rectangles; Jacobi seed 2; Chebyshev / PPCG seed 3 with 20 CG presteps, tl_ch_cg_epslim large
+so that the switch of tea_solve.f90:160-174 comes right after them, PPCG 10 inner steps), a
+step capped at --iters iterations (default 100 / 100 / 30), cell-iterations/s with the
+reference's iteration count (PPCG: outer iterations, each with its inner steps).
 
 value  : device time (CUDA events on the solver stream) of the K timed steps, inputs
-         resident in HBM (every step reads ~14 fields of 0.54 GB: larger than L2).
+         resident in HBM (every field is larger than L2).
 e2e    : the same steps through the C ABI with host buffers, host wall clock: every step's
-         density/energy copied from pinned host memory and its energy copied back, the copies
-         pipelined on their own streams (tl_stage_state two steps ahead, tl_fetch_field) so
-         they overlap the solves; e2e.synchronous is the upload/solve/download form.
-roofline: the dominant kernel (fused p-update + matvec + p.w sweep) timed per launch with
-         CUDA events during the timed steps, against 64 B/cell of compulsory traffic (the
-         p update and matvec streams plus the deferred u += alpha p of the previous step).
-cpu_baseline: the CPU port (oracle/, OpenMP over all host cores) on a bounded sample of
-         the same workload (one time-step solve capped at --cpu-iters iterations).
+         density/energy copied from pinned host memory and its energy copied back.  Two forms
+         exist: synchronous (upload, solve, download) and pipelined (tl_stage_state two steps
+         ahead on an upload stream, tl_fetch_field on a download stream, so the copies overlap
+         the solves).  One untimed step of each picks the form the timed steps use; the other
+         form is timed too and reported beside it.
+roofline: the dominant kernel of the line timed per launch with CUDA events recorded on the
+         solver stream during the timed steps, against its algorithmic bytes per cell;
+         `traffic` from the ncu capture summarised in profiles/roofline_traffic.json.
+cpu_baseline: the CPU port of the reference kernels (oracle/, OpenMP over all host cores) on
+         a bounded sample of the same workload (steps capped at --cpu-iters iterations; the
+         solver lines use the GPU's own window).
 
---impl reference times that CPU port alone as the reference arm.  Under torchrun (N>1)
-every rank runs an independent replica of the workload on its own GPU (the solve has no
-multi-GPU decomposition here), barrier + max-over-ranks time.
+--impl reference times that CPU port alone as the reference arm, with the same config dict
+(the sample window is reported beside it).  Under torchrun (N>1) every rank runs an
+independent replica of the workload on its own GPU (the solve has no multi-GPU decomposition
+here), barrier + max-over-ranks time.
 """
 from __future__ import annotations
 
@@ -40,72 +51,126 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# compulsory traffic of the fused sweep: r, p_old, Kx, Ky, u read; p, w, u written (8 B each).
-# The u += alpha p of the previous step is folded into it; Di (stored, 8 B more) is not
-# counted because the reference recomputes it from Kx, Ky.
-BYTES_PER_CELL_MATVEC = 64
 BYTES_PER_CELL_IT = 96      # whole FP64 CG iteration (12 streams)
-FP64_OPS_MATVEC = 8         # FP64 operations per cell of the matvec sweep: p update 1, A p 5, p.w 1, deferred u 1
 FP64_OPS_PER_CLOCK_SM = 2   # FP64 pipe peak that ncu reports for GB300: 2 thread-operations per clock per SM
 FALLBACK_HBM_GBS = 6800.0
 
+# Dominant kernel of each line: timer id (tl_profile), what it is, algorithmic bytes per cell per
+# launch, FP64 operations per cell per launch.
+#  cg        fused sweep 1: r, p_old, Kx, Ky, u read; p, w, u written (the u += alpha p of the
+#            previous iteration folded in; Di, stored, is not counted because the reference
+#            recomputes it); p update 1, A p 5, p.w 1, deferred u 1 FP64 operations
+#  jacobi    u0, un, Kx, Ky read; u written; 15 operations (the reference's bits: every product
+#            and sum rounded separately, the quotient by a corrected reciprocal)
+#  chebyshev u, u0, p, Kx, Ky read; p, u written; A u 5, r 1, p 2, u 1
+#  ppcg      sd, rtemp, utemp, Kx, Ky read; sd, rtemp, utemp written; A sd 5, rtemp 1, sd 2, utemp 1
+KERNELS = {
+    "cg": ("cg_matvec", "k_fused_cg_w (p = r + beta p, w = A p, p.w, deferred u += alpha p)", 64, 8),
+    "jacobi": ("jacobi", "k_fused_jacobi (u = (u0 + neighbour fluxes of un) / denominator, sum |u - un|)", 40, 15),
+    "chebyshev": ("cheby_iterate", "FP64 Chebyshev iteration (k_cheby_wr: w = A u, r = u0 - w; k_cheby_iter_pu: "
+                                   "p = a p + b r, u += p)", 56, 9),
+    "ppcg": ("ppcg_inner", "FP64 PPCG inner step (k_ppcg_inner_r: rtemp -= A sd; k_ppcg_inner_s: sd = a sd + b rtemp, "
+                           "utemp += sd)", 64, 9),
+}
+# The precision form's dominant kernels (FP32 streams, 4 B each): the FP32 CG sweep 1 (r, p_old,
+# Kx, Ky, d read; p, w, d written) and one blocked FP32 polynomial step of Chebyshev (d, r, p, Kx,
+# Ky read; p, d written) or PPCG (sd, rtemp, utemp, Kx, Ky read; sd, rtemp, utemp written).
+MIXED_KERNELS = {
+    "cg": ("mix_matvec", "k_mix_w (FP32 p update + matvec + p.w + deferred d += alpha p)", 32),
+    "chebyshev": ("poly_step", "k_poly_tb (temporally blocked FP32 Chebyshev steps), per step", 28),
+    "ppcg": ("poly_step", "k_poly_tb (temporally blocked FP32 PPCG inner steps), per step", 32),
+}
+DEFAULT_ITERS = {"cg": 500, "jacobi": 100, "chebyshev": 100, "ppcg": 30}
 
-def parse():
+
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cells", type=int, default=8192)
-    ap.add_argument("--iters", type=int, default=500, help="CG iterations per step (tl_max_iters)")
-    ap.add_argument("--cpu-iters", type=int, default=5, help="CG iterations per CPU sample step")
+    ap.add_argument("--solver", default="cg", choices=["cg", "jacobi", "chebyshev", "ppcg"],
+                    help="cg: the 8192^2 headline; jacobi / chebyshev / ppcg: the 4096^2 workloads")
+    ap.add_argument("--cells", type=int, default=None, help="mesh size (default 8192 for cg, 4096 otherwise)")
+    ap.add_argument("--iters", type=int, default=None, help="iterations per step (tl_max_iters)")
+    ap.add_argument("--cpu-iters", type=int, default=None,
+                    help="iterations per CPU sample step (default 50 for cg, the GPU window otherwise)")
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
-                    help="form timed in the main loop (mixed: FP32 CG steps with FP64 residual replacement)")
+                    help="form timed in the main loop (mixed: FP32 steps inside FP64 refinement)")
     ap.add_argument("--no-mixed-compare", action="store_true",
                     help="skip the full-solve FP64 vs mixed time-to-solution comparison")
     ap.add_argument("--delta", type=float, default=0.0, help="mixed: residual replacement factor (0: library default)")
     ap.add_argument("--adjoint", action="store_true",
                     help="instead of the CG line: the adjoint problem (2048^2, 10 steps; gradient of "
                          "sum (u - u_target)^2 wrt density), forward + reverse time and finite-difference checks")
-    ap.add_argument("--fd-cells", type=int, default=8, help="adjoint: cells for the per-cell difference check")
-    ap.add_argument("--solver", default="cg", choices=["cg", "jacobi", "chebyshev", "ppcg"],
-                    help="jacobi / chebyshev / ppcg: instead of the CG line, time steps of that solver on the "
-                         "4096^2 workloads (Jacobi: 8 rectangles, seed 2, capped at --iters; Chebyshev / PPCG: "
-                         "seed 3, 20 CG presteps, PPCG 10 inner steps, solved to tl_eps) and report per-kernel "
-                         "GB/s from a separately profiled step")
+    ap.add_argument("--fd-cells", type=int, default=16, help="adjoint: cells for the per-cell difference check")
     ap.add_argument("--compare-fp64", action="store_true",
-                    help="chebyshev / ppcg with --precision mixed: also solve the first time step from the "
-                         "generated state in both forms and report time, true residual and the mixed form's "
-                         "field-summary and per-cell u differences")
-    ap.add_argument("--ch-cg-epslim", type=float, default=None,
-                    help="chebyshev / ppcg: override tl_ch_cg_epslim (the error below which CG hands over "
-                         "after its presteps; a large value switches right after them)")
-    return ap.parse_args()
+                    help="chebyshev / ppcg: also solve the first time step from the generated state to tl_eps "
+                         "in the FP64 and the mixed form and report time, true residual and their differences")
+    a = ap.parse_args(argv)
+    if a.cells is None:
+        a.cells = 8192 if a.solver == "cg" else 4096
+    if a.iters is None:
+        a.iters = DEFAULT_ITERS[a.solver]
+    if a.cpu_iters is None:
+        a.cpu_iters = 50 if a.solver == "cg" else a.iters
+    return a
 
 
 def workload(args):
+    """The deck of the line: config 5 (cg), config 2 (jacobi) or config 3 (chebyshev / ppcg)."""
     from tealeaf_ref_gb300 import deck as dk
 
-    d = dk.config_deck(5, cells=args.cells)
+    if args.solver == "cg":
+        d = dk.config_deck(5, cells=args.cells)
+    elif args.solver == "jacobi":
+        d = dk.config_deck(2, solver="jacobi", cells=args.cells)
+    else:
+        d = dk.config_deck(3, solver=args.solver, cells=args.cells)
+        d.ch_cg_presteps = 20
+        d.ch_cg_epslim = 1e30
     d.max_iters = args.iters
     return d
 
 
-def config_json(args, d):
+def workload_text(args):
+    n = args.cells
+    if args.solver == "cg":
+        return ("TeaLeaf implicit diffusion, FP64 CG, %dx%d cells, 16 rectangles + 4 circles (seed 5), "
+                "reciprocal-density keyword, dt 0.004, tl_eps 1e-15; step = one tea_leaf() solve capped at "
+                "%d iterations" % (n, n, args.iters))
+    if args.solver == "jacobi":
+        return ("TeaLeaf implicit diffusion, FP64 Jacobi, %dx%d cells, 8 rectangles (seed 2), reciprocal-density "
+                "keyword, dt 0.004, tl_eps 1e-15; step = one tea_leaf() solve capped at %d iterations"
+                % (n, n, args.iters))
+    extra = ", 10 inner steps" if args.solver == "ppcg" else ""
+    return ("TeaLeaf implicit diffusion, FP64 %s, %dx%d cells, 8 rectangles (seed 3), reciprocal-density keyword, "
+            "dt 0.004, tl_eps 1e-15, 20 CG presteps then the switch%s; step = one tea_leaf() solve capped at %d "
+            "iterations" % ("Chebyshev" if args.solver == "chebyshev" else "PPCG", n, n, extra, args.iters))
+
+
+def config_json(args, world=None):
+    """The config dict of the line, identical in both arms."""
+    if world is None:
+        world = int(os.environ.get("WORLD_SIZE", "1"))
     return {
-        "workload": "TeaLeaf implicit diffusion, FP64 CG, %dx%d cells, 16 rectangles + 4 circles (seed 5), "
-                    "reciprocal-density keyword, dt 0.004, tl_eps 1e-15; step = one tea_leaf() solve capped at "
-                    "%d iterations" % (args.cells, args.cells, args.iters),
+        "workload": workload_text(args),
         "cells": args.cells * args.cells,
         "iterations_per_step": args.iters,
-        "solver": "cg",
-        "precision": "fp64",
-        "l2": "inputs larger than L2 (each field %.0f MB, ~14 fields touched per step)" % (
-            (args.cells + 2) * (args.cells + 18) * 8 / 1e6),
+        "solver": args.solver,
+        "precision": args.precision,
+        "l2": "inputs larger than L2 (each field %.0f MB)" % ((args.cells + 2) * (args.cells + 20) * 8 / 1e6),
+        "parallelism": "replicas" if world > 1 else "single",
     }
+
+
+def metric_name(args):
+    names = {"cg": "CG", "jacobi": "Jacobi", "chebyshev": "Chebyshev", "ppcg": "PPCG"}
+    form = "FP64" if args.precision == "fp64" else "FP32 steps with FP64 refinement"
+    return "%s cell-iterations/s (%s, %d^2)" % (names[args.solver], form, args.cells)
 
 
 def measured_peaks():
@@ -124,12 +189,15 @@ def measured_peaks():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def ncu_traffic():
+def ncu_traffic(kernel_key):
+    """DRAM bytes per cell of a launch of the line's kernel from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "roofline_traffic.json")
-    if os.path.exists(p):
-        with open(p) as f:
-            return json.load(f)
-    return None
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        j = json.load(f)
+    k = j.get("kernels", {}).get(kernel_key)
+    return k
 
 
 class Clocks:
@@ -191,7 +259,8 @@ class Clocks:
 
 
 def cpu_port_steps(d, iters, steps, warmup, density=None, energy=None):
-    """Time the OpenMP CPU port (oracle) on one-step solves capped at `iters` iterations."""
+    """Time the OpenMP CPU port (oracle) on one-step solves capped at `iters` iterations.
+    Returns (seconds, iterations, cores)."""
     from oracle import oracle
 
     cores = os.cpu_count() or 1
@@ -200,9 +269,9 @@ def cpu_port_steps(d, iters, steps, warmup, density=None, energy=None):
     c = oracle.Chunk(dd.x_cells, dd.y_cells, dd.halo_depth, dd.xmin, dd.ymin, dd.xmax, dd.ymax, dd.coefficient,
                      dd.precond_id, dd.reflective_boundary, threaded=True)
     if density is not None:
-        # state taken from the GPU generator (the CPU generator is slow at this size); halo
-        # cells get the ambient density, as generate_chunk gives them (boundary faces are
-        # zeroed afterwards, but their coefficient is still formed from it)
+        # state taken from the GPU generator; halo cells get the ambient density, as
+        # generate_chunk gives them (boundary faces are zeroed afterwards, but their
+        # coefficient is still formed from it)
         dens = c.array("density")
         dens[...] = 100.0
         c.interior("density")[...] = density
@@ -217,8 +286,13 @@ def cpu_port_steps(d, iters, steps, warmup, density=None, energy=None):
         t0 = time.perf_counter()
         info = c.tea_leaf(dd)
         times.append(time.perf_counter() - t0)
-        its += info.n_exit if info.n_exit <= iters else iters
+        its += min(info.n_exit, iters)
     return sum(times), its, cores
+
+
+def cpu_sample_text(args, steps, iters):
+    return ("%d timed one-step solves capped at %d iterations each (%s), %dx%d cells, OpenMP CPU port of the "
+            "reference kernels (oracle/)" % (steps, iters, args.solver, args.cells, args.cells))
 
 
 def mixed_vs_fp64(chunk, d, args):
@@ -259,8 +333,40 @@ def mixed_vs_fp64(chunk, d, args):
     out["u_max_rel_diff"] = float(np.max(np.abs(umx - u64) / np.abs(u64)))
     out["workload"] = "first time step of the %dx%d workload from its generated state, tl_eps %g" % (
         args.cells, args.cells, full.eps)
+    out["against_oracle"] = ("the FP64 form is held to the oracle at this size on capped windows "
+                             "(tests/test_gpu_configs.py); the mixed form is compared with the FP64 form here")
     chunk.upload_state(dens0, ener0)
     return out
+
+
+def solve_time_to_solution(d, args):
+    """Chebyshev / PPCG: the first time step from the generated state solved to tl_eps 1e-15 in
+    the FP64 and the mixed form (the 4096^2 workload's time to solution)."""
+    import numpy as np
+
+    from tealeaf_ref_gb300 import native
+
+    full = d.replace(max_iters=50000, ch_cg_epslim=1.0)
+    first = {}
+    for form in ("fp64", "mixed"):
+        o = native.opts_from_deck(full, form)
+        o.check_result = 1
+        with native.Chunk.from_deck(full) as c:
+            i = c.tea_leaf(o, full.initial_timestep)
+            first[form] = (i, c.field_summary(), c.download("u"))
+    (i64, s64, u64), (imx, smx, umx) = first["fp64"], first["mixed"]
+    return {
+        "workload": "first time step of the %dx%d workload from its generated state, tl_eps 1e-15, "
+                    "tl_ch_cg_epslim 1 (the deck default)" % (args.cells, args.cells),
+        "fp64": {"seconds": i64.solve_seconds, "iterations": i64.reported_iterations,
+                 "relative_true_residual": i64.exact_error / i64.initial_residual},
+        "mixed": {"seconds": imx.solve_seconds, "iterations": imx.reported_iterations, "cg_presteps": imx.cg_calc_steps,
+                  "relative_true_residual": imx.exact_error / imx.initial_residual,
+                  "stop": native.STOP_REASONS.get(imx.stop_reason, str(imx.stop_reason))},
+        "time_ratio_mixed_over_fp64": imx.solve_seconds / i64.solve_seconds,
+        "field_summary_max_rel_diff": float(max(abs(a - b) / abs(b) for a, b in zip(smx, s64))),
+        "u_max_rel_diff": float((np.abs(umx - u64) / np.abs(u64)).max()),
+    }
 
 
 def run_adjoint(args):
@@ -336,112 +442,9 @@ def run_adjoint(args):
     print(json.dumps(out), flush=True)
 
 
-# Compulsory bytes per cell of one launch (or one step) of each timed kernel: FP64 Chebyshev
-# iterate 56 B (u, u0, p, Kx, Ky read; p, u written), PPCG inner step 64 B (sd, rtemp, utemp,
-# Kx, Ky read; sd, rtemp, utemp written), Jacobi 40 B (u0, un, Kx, Ky read; u written); the
-# FP32 forms at 4 B per stream: PPCG inner step 32 B, Chebyshev step on a correction 28 B
-# (d, r, p, Kx, Ky read; p, d written); FP32 CG sweeps 32 B (r, p_old, Kx, Ky, d read; p, w, d
-# written) and 12 B (w, r read; r written).
-KERNEL_BYTES = {"cheby_iterate": 56, "ppcg_inner": 64, "jacobi": 40, "mix_matvec": 32, "mix_update": 12,
-                "cg_matvec": 64, "cg_update": 24}
-POLY_BYTES = {"ppcg": 32, "chebyshev": 28}
-
-
-def run_solver(args):
-    """Time steps of the Jacobi, Chebyshev or PPCG solver (FP64 or mixed form) on the 4096^2
-    workloads; per-kernel times come from one more step run with the kernel timers on (the
-    host-driven loops wait for each timed launch, so that step is not part of the timing)."""
-    from tealeaf_ref_gb300 import deck as dk
-    from tealeaf_ref_gb300 import native
-
-    cells_n = args.cells if args.cells != 8192 else 4096
-    if args.solver == "jacobi":
-        d = dk.config_deck(2, solver="jacobi", cells=cells_n)
-        d.max_iters = args.iters
-    else:
-        d = dk.config_deck(3, solver=args.solver, cells=cells_n)
-        d.ch_cg_presteps = 20
-        if args.ch_cg_epslim is not None:
-            d.ch_cg_epslim = args.ch_cg_epslim
-    opts = native.opts_from_deck(d, args.precision)
-    dt = d.initial_timestep
-    cells = cells_n * cells_n
-    with native.Chunk.from_deck(d) as c:
-        for _ in range(args.warmup):
-            c.tea_leaf(opts, dt)
-        infos = []
-        with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
-            for _ in range(args.steps):
-                infos.append(c.tea_leaf(opts, dt))
-        dev_s = sum(i.solve_seconds for i in infos)
-        c.profile(True)
-        pinfo = c.tea_leaf(opts, dt)
-        kernels = {}
-        for name, kid in native.KERNEL_TIMERS.items():
-            ms, n = c.profile_read(name)
-            if not n:
-                continue
-            basis = (POLY_BYTES[args.solver] if name == "poly_step" else KERNEL_BYTES[name])
-            avg = ms / n * 1e-3
-            kernels[name] = {"launches": n, "ms_avg": 1e3 * avg, "bytes_per_cell": basis,
-                             "gbs": basis * cells / avg / 1e9}
-        c.profile(False)
-    compare = None
-    if args.compare_fp64 and args.precision == "mixed" and args.solver != "jacobi":
-        first = {}
-        for form in ("fp64", "mixed"):
-            o = native.opts_from_deck(d, form)
-            o.check_result = 1
-            with native.Chunk.from_deck(d) as c:
-                i = c.tea_leaf(o, dt)
-                first[form] = (i, c.field_summary(), c.download("u"))
-        (i64, s64, u64), (imx, smx, umx) = first["fp64"], first["mixed"]
-        compare = {
-            "workload": "first time step of the %dx%d workload from its generated state, tl_eps 1e-15" % (cells_n,
-                                                                                                        cells_n),
-            "fp64": {"seconds": i64.solve_seconds, "iterations": i64.reported_iterations,
-                     "relative_true_residual": i64.exact_error / i64.initial_residual},
-            "mixed": {"seconds": imx.solve_seconds, "iterations": imx.reported_iterations,
-                      "cg_presteps": imx.cg_calc_steps,
-                      "relative_true_residual": imx.exact_error / imx.initial_residual,
-                      "stop": native.STOP_REASONS.get(imx.stop_reason, str(imx.stop_reason))},
-            "time_ratio_mixed_over_fp64": imx.solve_seconds / i64.solve_seconds,
-            "field_summary_max_rel_diff": float(max(abs(a - b) / abs(b) for a, b in zip(smx, s64))),
-            "u_max_rel_diff": float((abs(umx - u64) / abs(u64)).max()),
-        }
-    peak, peak_kind = measured_peaks()
-    for k in kernels.values():
-        k["frac_of_peak"] = k["gbs"] / peak
-    out = {
-        "metric": "%s time per time step (%s, %d^2)" % (args.solver, args.precision, cells_n),
-        "value": dev_s / args.steps,
-        "unit": "s",
-        "higher_is_better": False,
-        "n_gpus": 1,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "iterations_per_step": [i.reported_iterations for i in infos],
-        "ppcg_inner_per_step": [i.ppcg_inner_iters for i in infos],
-        "cg_presteps_per_step": [i.cg_calc_steps for i in infos],
-        "cell_iterations_per_s": cells * sum(i.reported_iterations for i in infos) / dev_s,
-        "kernels": kernels,
-        "peak_gbs": peak,
-        "peak_source": peak_kind,
-        "profiled_step_iterations": pinfo.reported_iterations,
-        "mixed_vs_fp64": compare,
-        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-        "data": "synthetic",
-        "clocks": clk.summary(),
-        "config": {"workload": "TeaLeaf implicit diffusion, %s (%s), %dx%d cells, 8 rectangles, reciprocal-density "
-                               "keyword, dt 0.004, tl_eps 1e-15%s" % (
-                                   args.solver, args.precision, cells_n, cells_n,
-                                   ", capped at %d iterations" % args.iters if args.solver == "jacobi" else
-                                   ", 20 CG presteps" + (", 10 PPCG inner steps" if args.solver == "ppcg" else ""))},
-    }
-    print(json.dumps(out), flush=True)
-
-
 def run_reference(args):
+    """The reference arm: the CPU port of the reference kernels on all host cores, on a bounded
+    sample of the same workload (steps capped at --cpu-iters iterations), rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -450,9 +453,10 @@ def run_reference(args):
     total, its, cores = cpu_port_steps(d, iters, args.steps, args.warmup)
     cells = args.cells * args.cells
     value = cells * its / total
+    sample = cpu_sample_text(args, args.steps, iters)
     out = {
         "impl": "reference",
-        "metric": "CG cell-iterations/s (FP64, %d^2)" % args.cells,
+        "metric": metric_name(args),
         "value": value,
         "unit": "cell-iterations/s",
         "n_gpus": args.gpus,
@@ -464,34 +468,108 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": dict(config_json(args, d), cpu_sample_iterations_per_step=iters),
+        "config": config_json(args),
+        "cpu_sample": {"iterations_per_step": iters, "steps": args.steps, "warmup_steps": args.warmup,
+                       "what": "each step is a bounded sample of the workload's step: the same solve capped at "
+                               "%d iterations" % iters},
         "cpu_baseline": {"value": value, "unit": "cell-iterations/s", "cores": cores, "kind": "port",
-                         "sample": "%d timed one-step solves capped at %d CG iterations each, %dx%d cells, "
-                                   "OpenMP CPU port of the reference kernels" % (args.steps, iters, args.cells,
-                                                                                 args.cells)},
+                         "sample": sample},
         "e2e": {"value": value, "unit": "cell-iterations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }
     print(json.dumps(out), flush=True)
 
 
-def main():
-    args = parse()
+def e2e_legs(chunk, opts, dt, args, grp, cells):
+    """End to end through the C ABI with pinned host buffers.  One untimed step of each form
+    (synchronous; pipelined) picks the form of the timed steps; the other form is then timed
+    too.  Returns the e2e dict and the host arrays (density, energy) for the CPU leg."""
+    from tealeaf_ref_gb300 import native, replicas
+
+    world = grp.world
+    pins = [native.PinnedArray((args.cells, args.cells)) for _ in range(3)]
+    dens, ener, out = (p.array for p in pins)
+    chunk.download("density", out=dens)
+    chunk.download("energy1", out=ener)
+    chunk.upload_state(dens, ener)
+    chunk.tea_leaf(opts, dt)
+
+    def sync_steps(n):
+        its, parts = 0, [0.0, 0.0, 0.0]
+        grp.barrier()
+        t0 = time.perf_counter()
+        for _ in range(n):
+            ta = time.perf_counter()
+            chunk.upload_state(dens, ener)
+            tb = time.perf_counter()
+            info = chunk.tea_leaf(opts, dt)
+            tc = time.perf_counter()
+            chunk.download("energy1", out=out)
+            td = time.perf_counter()
+            its += min(info.n_exit, args.iters)
+            parts[0] += tb - ta
+            parts[1] += info.solve_seconds
+            parts[2] += td - tc
+        wall = grp.max(time.perf_counter() - t0)
+        return wall, its, {k: 1e3 * v / n for k, v in zip(("upload", "solve_device", "download"), parts)}
+
+    def pipelined_steps(n):
+        its, parts = 0, [0.0, 0.0, 0.0, 0.0]
+        grp.barrier()
+        t0 = time.perf_counter()
+        for _ in range(min(2, n)):
+            chunk.stage_state(dens, ener)
+        for s in range(n):
+            ta = time.perf_counter()
+            chunk.take_staged()
+            tb = time.perf_counter()
+            info = chunk.tea_leaf(opts, dt)
+            tc = time.perf_counter()
+            its += min(info.n_exit, args.iters)
+            chunk.fetch("energy1", out)
+            if s + 2 < n:
+                chunk.stage_state(dens, ener)
+            td = time.perf_counter()
+            parts[0] += tb - ta
+            parts[1] += tc - tb
+            parts[2] += info.solve_seconds
+            parts[3] += td - tc
+        chunk.wait_transfers()
+        wall = grp.max(time.perf_counter() - t0)
+        return wall, its, {k: 1e3 * v / n for k, v in zip(("take", "solve_host", "solve_device", "fetch_stage"), parts)}
+
+    forms = {"synchronous": sync_steps, "pipelined": pipelined_steps}
+    # the untimed pick: one step of each form
+    probe = {name: fn(1)[0] for name, fn in forms.items()}
+    chosen = min(probe, key=probe.get)
+    other = "pipelined" if chosen == "synchronous" else "synchronous"
+    with Clocks(grp.local) as clk:
+        wall, its, parts = forms[chosen](args.steps)
+    o_wall, o_its, o_parts = forms[other](args.steps)
+    e2e = {"value": replicas.whole_job_rate(world, cells, its, wall), "unit": "cell-iterations/s",
+           "h2d_bytes_per_step": 2 * cells * 8, "d2h_bytes_per_step": cells * 8,
+           "ms_per_step": 1e3 * wall / args.steps, "form": chosen,
+           "form_choice": "the faster of one untimed step of each form: %s" % (
+               ", ".join("%s %.1f ms" % (k, 1e3 * v) for k, v in probe.items())),
+           "ms_per_step_parts": parts,
+           "other_form": {"form": other, "value": replicas.whole_job_rate(world, cells, o_its, o_wall),
+                          "ms_per_step": 1e3 * o_wall / args.steps, "ms_per_step_parts": o_parts},
+           "clocks": clk.summary()}
+    return e2e, dens, ener, pins
+
+
+def main(argv=None):
+    args = parse(argv)
     if args.impl == "reference":
         run_reference(args)
         return
     if args.adjoint:
         run_adjoint(args)
         return
-    if args.solver != "cg":
-        run_solver(args)
-        return
     from tealeaf_ref_gb300 import replicas
 
     grp = replicas.init()
     world, rank, local = grp.world, grp.rank, grp.local
-
-    import numpy as np
 
     from tealeaf_ref_gb300 import native
 
@@ -500,146 +578,97 @@ def main():
     opts = native.opts_from_deck(d, args.precision, inner_tol=args.delta)
     dt = d.initial_timestep
     cells = args.cells * args.cells
+    if args.precision == "mixed" and args.solver == "jacobi":
+        raise SystemExit("the precision form is built for CG, Chebyshev and PPCG")
+    timer, kernel_text, kbytes, kops = KERNELS[args.solver]
+    if args.precision == "mixed":
+        timer, kernel_text, kbytes = MIXED_KERNELS[args.solver]
 
     chunk = native.Chunk.from_deck(d)
     for _ in range(args.warmup):
         chunk.tea_leaf(opts, dt)
 
-    barrier = grp.barrier
-    max_over_ranks = grp.max
-
-    # ---- device-resident timed region ----
+    # ---- device-resident timed region (per-launch timers on, CUDA events on the solve stream) ----
     chunk.profile(True)
-    barrier()
+    grp.barrier()
     infos = []
     with Clocks(local) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
             infos.append(chunk.tea_leaf(opts, dt))
         wall = time.perf_counter() - t0
-    barrier()
+    grp.barrier()
     dev_s = sum(i.solve_seconds for i in infos)
     its = sum(min(i.n_exit, args.iters) for i in infos)
     launches = sum(i.kernel_launches for i in infos)
-    mv_ms, mv_n = chunk.profile_read("cg_matvec")
+    k_ms, k_n = chunk.profile_read(timer)
     up_ms, up_n = chunk.profile_read("cg_update")
     chunk.profile(False)
-    t_max = max_over_ranks(dev_s)
+    t_max = grp.max(dev_s)
     value = replicas.whole_job_rate(world, cells, its, t_max)
 
     # ---- end to end through the C ABI with host buffers ----
-    e2e = None
+    e2e, dens, ener, pins = (None, None, None, None)
     if not args.no_e2e:
-        pins = [native.PinnedArray((args.cells, args.cells)) for _ in range(3)]
-        dens, ener, out = (p.array for p in pins)
-        chunk.download("density", out=dens)
-        chunk.download("energy1", out=ener)
-        chunk.upload_state(dens, ener)
-        chunk.tea_leaf(opts, dt)
-        barrier()
-        # Synchronous form: upload, solve, download, one after the other.
-        s_its = 0
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            chunk.upload_state(dens, ener)
-            s_its += min(chunk.tea_leaf(opts, dt).n_exit, args.iters)
-            chunk.download("energy1", out=out)
-        s_wall = max_over_ranks(time.perf_counter() - t0)
-        barrier()
-        # Pipelined form (the headline): each step's inputs are staged two steps ahead on the
-        # upload stream and its energy is fetched on the download stream, so the copies run
-        # during the solves.  Every step still moves its own inputs and result across the link.
-        e_its = 0
-        parts = [0.0, 0.0, 0.0, 0.0]  # take (host), solve (host), solve (device), fetch + stage (host)
-        with Clocks(local) as clk_e2e:
-            t0 = time.perf_counter()
-            for _ in range(min(2, args.steps)):
-                chunk.stage_state(dens, ener)
-            for s in range(args.steps):
-                ta = time.perf_counter()
-                chunk.take_staged()
-                tb = time.perf_counter()
-                info = chunk.tea_leaf(opts, dt)
-                tc = time.perf_counter()
-                e_its += min(info.n_exit, args.iters)
-                chunk.fetch("energy1", out)
-                if s + 2 < args.steps:
-                    chunk.stage_state(dens, ener)
-                td = time.perf_counter()
-                parts[0] += tb - ta
-                parts[1] += tc - tb
-                parts[2] += info.solve_seconds
-                parts[3] += td - tc
-            chunk.wait_transfers()
-            e_wall = time.perf_counter() - t0
-        barrier()
-        e_wall = max_over_ranks(e_wall)
-        e2e = {"value": replicas.whole_job_rate(world, cells, e_its, e_wall), "unit": "cell-iterations/s",
-               "h2d_bytes_per_step": 2 * cells * 8, "d2h_bytes_per_step": cells * 8,
-               "ms_per_step": 1e3 * e_wall / args.steps, "transfers": "pipelined (tl_stage_state/tl_fetch_field)",
-               "ms_per_step_parts": {k: 1e3 * v / args.steps for k, v in
-                                     zip(("take", "solve_host", "solve_device", "fetch_stage"), parts)},
-               "synchronous": {"value": replicas.whole_job_rate(world, cells, s_its, s_wall),
-                               "ms_per_step": 1e3 * s_wall / args.steps},
-               "clocks": clk_e2e.summary()}
+        e2e, dens, ener, pins = e2e_legs(chunk, opts, dt, args, grp, cells)
 
     peak, peak_kind = measured_peaks()
-    t_launch = mv_ms / mv_n * 1e-3 if mv_n else None
-    achieved = BYTES_PER_CELL_MATVEC * cells / t_launch / 1e9 if t_launch else None
-    traffic = ncu_traffic()
-    per_launch_traffic = None
-    if traffic and traffic.get("cells"):
-        per_launch_traffic = traffic["bytes_per_cell"] * cells
+    t_launch = k_ms / k_n * 1e-3 if k_n else None
+    achieved = kbytes * cells / t_launch / 1e9 if t_launch else None
+    traffic = ncu_traffic(args.solver if args.precision == "fp64" else None)
     roofline = {
         "bound": "hbm",
-        "kernel": "k_fused_cg_w (p = r + beta p, w = A p, p.w)",
+        "kernel": kernel_text,
         "achieved": achieved,
         "peak": peak,
         "unit": "GB/s",
         "frac": achieved / peak if achieved else None,
         "peak_source": peak_kind,
-        "traffic": per_launch_traffic,
-        "algorithmic_bytes_per_cell": BYTES_PER_CELL_MATVEC,
-        "launch_ms": mv_ms / mv_n if mv_n else None,
-        "launches": mv_n,
-        "update_kernel_launch_ms": up_ms / up_n if up_n else None,
-        "iteration_gbs_at_96B": BYTES_PER_CELL_IT * cells * its / dev_s / 1e9 if dev_s else None,
-        "note": "FP64 issue rate (measured 0.60 T DFMA/s) bounds the sweep before HBM does",
+        "traffic": traffic["bytes_per_cell"] * cells if traffic else None,
+        "traffic_source": traffic.get("source") if traffic else None,
+        "algorithmic_bytes_per_cell": kbytes,
+        "launch_ms": k_ms / k_n if k_n else None,
+        "launches": k_n,
     }
-    if t_launch:
+    if args.solver == "cg":
+        roofline["update_kernel_launch_ms"] = up_ms / up_n if up_n else None
+        roofline["iteration_gbs_at_96B"] = BYTES_PER_CELL_IT * cells * its / dev_s / 1e9 if dev_s else None
+        if dev_s:
+            roofline["iteration_frac_at_96B"] = roofline["iteration_gbs_at_96B"] / peak
+    if t_launch and args.precision == "fp64":
         import torch
 
         sms = torch.cuda.get_device_properties(local).multi_processor_count
         mhz = clk.summary().get("sm_max_mhz") or 2070.0
         fp64_peak = FP64_OPS_PER_CLOCK_SM * sms * mhz * 1e6
-        fp64_achieved = FP64_OPS_MATVEC * cells / t_launch
+        fp64_achieved = kops * cells / t_launch
         roofline["fp64_issue"] = {
-            "ops_per_cell": FP64_OPS_MATVEC, "achieved_tops": fp64_achieved / 1e12, "peak_tops": fp64_peak / 1e12,
+            "ops_per_cell": kops, "achieved_tops": fp64_achieved / 1e12, "peak_tops": fp64_peak / 1e12,
             "frac": fp64_achieved / fp64_peak,
             "peak_source": "%d FP64 thread-ops per clock per SM (ncu's FP64 pipe peak) x %d SMs x %.0f MHz"
                            % (FP64_OPS_PER_CLOCK_SM, sms, mhz)}
+        roofline["note"] = "FP64 issue rate (0.63 T ops/s) bounds the sweep before HBM does"
 
-    mixed_cmp = None
-    if rank == 0 and world == 1 and not args.no_mixed_compare:
-        mixed_cmp = mixed_vs_fp64(chunk, d, args)
+    extra = None
+    if rank == 0 and world == 1:
+        if args.solver == "cg" and not args.no_mixed_compare:
+            extra = ("mixed_vs_fp64", mixed_vs_fp64(chunk, d, args))
+        elif args.solver in ("chebyshev", "ppcg") and args.compare_fp64:
+            extra = ("time_to_solution", solve_time_to_solution(d, args))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
-            total, cits, cores = cpu_port_steps(d, args.cpu_iters, args.cpu_steps, 1, dens if e2e else None,
-                                                ener if e2e else None)
+            total, cits, cores = cpu_port_steps(d, args.cpu_iters, args.cpu_steps, 1, dens, ener)
             cpu = {"value": cells * cits / total, "unit": "cell-iterations/s", "cores": cores, "kind": "port",
-                   "sample": "%d one-step solves capped at %d CG iterations, %dx%d cells, OpenMP CPU port of the "
-                             "reference kernels (oracle/)" % (args.cpu_steps, args.cpu_iters, args.cells,
-                                                              args.cells)}
+                   "sample": cpu_sample_text(args, args.cpu_steps, args.cpu_iters)}
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "cell-iterations/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": "failed: %s" % e}
 
     if rank == 0:
         out = {
-            "metric": ("CG cell-iterations/s (FP64, %d^2)" % args.cells if args.precision == "fp64" else
-                       "CG cell-iterations/s (FP32 steps with FP64 residual replacement, %d^2)" % args.cells),
+            "metric": metric_name(args),
             "value": value,
             "unit": "cell-iterations/s",
             "n_gpus": world,
@@ -651,17 +680,23 @@ def main():
             "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic",
-            "config": dict(config_json(args, d), parallelism="replicas" if world > 1 else "single",
-                           precision=args.precision),
+            "config": config_json(args, world),
+            "iterations_per_step": [i.reported_iterations for i in infos],
             "roofline": roofline,
             "cpu_baseline": cpu,
-            "mixed_vs_fp64": mixed_cmp,
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "wall_s_timed": wall,
         }
+        if args.solver == "ppcg":
+            out["ppcg_inner_per_step"] = [i.ppcg_inner_iters for i in infos]
+        if extra:
+            out[extra[0]] = extra[1]
         print(json.dumps(out), flush=True)
+    if pins:
+        for p in pins:
+            p.close()
     chunk.close()
     grp.close()
 

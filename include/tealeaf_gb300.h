@@ -5,7 +5,7 @@
  * that the reference's solver drivers (tea_leaf_*.f90) call under
  * IF (use_fortran_kernels); the citation on each line names that subroutine.  A
  * Fortran driver binds these with BIND(C), VALUE scalars and TYPE(C_PTR) for the
- * context (see INTEGRATION.md).
+ * context.
  *
  * Conventions
  *  - One context (tl_ctx) owns one chunk of x_cells * y_cells cells resident in
@@ -255,9 +255,12 @@ int tl_update_halo(tl_ctx* ctx, int field_mask, int depth);
  * under a fixed memory budget, or must not call cudaMalloc/cudaFree inside their time loop.
  * Needs no tl_ctx and allocates nothing: the row sums of p.w use a fixed device array of
  * 16384 + 32 doubles inside the library, so y_cells must be <= 16384 (larger sizes are
- * rejected with TL_ERR_ARG).  The first call on each device, made with that device current,
- * looks up the array's device address.  Runs on the default stream and returns after pw is
- * on the host.  Calls that overlap on the GPU share the array and race. */
+ * rejected with TL_ERR_ARG).  Each call looks up the array's device address on the current
+ * device; the first call on a device also loads the library's device code there, so make it
+ * before any stream capture.  Runs on the legacy default stream and returns after pw is on
+ * the host.  That stream does not wait for streams created with cudaStreamNonBlocking (e.g.
+ * OpenACC async queues): finish the writes of p, Kx, Ky and Di there first.  Calls that
+ * overlap on the GPU share the array and race. */
 int tl_cg_calc_w_noalloc(int x_cells, int y_cells, int halo_depth, const double* p, double* w, const double* kx,
                          const double* ky, const double* di, double rx, double ry, double* pw);
 

@@ -51,8 +51,15 @@ class _Info(C.Structure):
                 ("eigmin", C.c_double), ("eigmax", C.c_double), ("status", C.c_int)]
 
 
-def lib(threaded: bool = False):
-    name = "liboracle_omp.so" if threaded else "liboracle.so"
+VARIANTS = {False: "liboracle.so", True: "liboracle_omp.so", "omp": "liboracle_omp.so",
+            "par": "liboracle_par.so"}
+
+
+def lib(threaded=False):
+    """threaded: False -- the serial checker (pinned bit-exact to the reference's outputs);
+    True / "omp" -- the OpenMP timing build (FMA contraction, the CPU baseline);
+    "par" -- the OpenMP checker (no contraction; global sums over per-thread partials)."""
+    name = VARIANTS[threaded]
     with _lock:
         if name in _libs:
             return _libs[name]

@@ -6,9 +6,11 @@
  * inside each expression follow the reference, and the file is compiled with
  * -ffp-contract=off, so that the serial build reproduces the reference's IEEE
  * (no-FMA, no-reassociation) benchmark outputs.  The OpenMP pragmas only take effect
- * in the separately-built timing variant (liboracle_omp.so, compiled as the reference
- * compiles its kernels: -O3 -funroll-loops with FMA contraction), whose results are
- * therefore not bit-identical to the serial build.
+ * in the separately-built variants: the timing variant (liboracle_omp.so, compiled as the
+ * reference compiles its kernels: -O3 -funroll-loops with FMA contraction), whose results
+ * are therefore not bit-identical to the serial build, and the parallel checker
+ * (liboracle_par.so, -ffp-contract=off), whose per-cell arithmetic is the serial build's
+ * and whose global sums add per-thread partials.
  *
  * Citations are file:line in the reference (UK-MAC/TeaLeaf_ref).
  */

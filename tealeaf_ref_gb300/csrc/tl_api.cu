@@ -71,12 +71,24 @@ struct tl_ctx {
   int first = 1;
   double eigmin = 0, eigmax = 0, theta = 0, cn = 0;
   bool have_coefs = false;
+  // Set-up cache: Kx, Ky, cx, cy, Di, Mi and the block factors depend only on density and dt
+  // (and the chunk's fixed geometry, coefficient keyword and boundary type).  They are valid
+  // for setup_dt while setup_valid; every entry point that can write density, Kx, Ky, Di or
+  // Mi clears the flag, so a solve rebuilds them exactly when the reference's per-step
+  // tea_leaf_common_init would produce different values.
+  bool setup_valid = false;
+  double setup_dt = 0.0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // per-launch timers of the fused loop kernels (tl_profile)
   static constexpr int BATCH = 16;
   bool prof = false;
   cudaEvent_t pev[3 * BATCH] = {};
-  cudaEvent_t qe0 = nullptr, qe1 = nullptr;  // one timed launch of a host-driven loop
+  // timed launches of the host-driven loops: event pairs recorded around each launch and read
+  // once QCAP are pending or the solve ends, so the host never waits for a single launch
+  static constexpr int QCAP = 256;
+  cudaEvent_t qev[2 * QCAP] = {};
+  int qid[QCAP] = {}, qcount[QCAP] = {};
+  int qn = 0;
   // CUDA graphs of one batch of the device-resident loops (captured once per set of kernel
   // arguments): the fused CG batch and the mixed-precision CG batch
   cudaGraphExec_t cg_exec = nullptr, mix_exec = nullptr;
@@ -197,20 +209,37 @@ int ensure_ch(tl_ctx* c, int n) {
   return TL_OK;
 }
 
-// Timers of the host-driven loops: prof_begin before a launch, prof_end after it waits for it
-// and adds its time to TL_KERNEL id (count units).  No-ops unless tl_profile is on.
+// Timers of the host-driven loops: prof_begin before a launch and prof_end after it record an
+// event pair on the solve stream; prof_flush (when QCAP pairs are pending, at the end of a
+// solve and in tl_profile_read) waits for the last one and adds each launch's time to its
+// TL_KERNEL id (count units).  No-ops unless tl_profile is on.
+int prof_flush(tl_ctx* c) {
+  if (c->qn == 0) return TL_OK;
+  CK(cudaEventSynchronize(c->qev[2 * c->qn - 1]));
+  for (int i = 0; i < c->qn; ++i) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->qev[2 * i], c->qev[2 * i + 1]));
+    c->prof_ms[c->qid[i]] += ms;
+    c->prof_n[c->qid[i]] += c->qcount[i];
+  }
+  c->qn = 0;
+  return TL_OK;
+}
 int prof_begin(tl_ctx* c) {
-  if (c->prof) CK(cudaEventRecord(c->qe0, c->stream));
+  if (!c->prof) return TL_OK;
+  if (c->qn == tl_ctx::QCAP) {
+    int rc = prof_flush(c);
+    if (rc) return rc;
+  }
+  CK(cudaEventRecord(c->qev[2 * c->qn], c->stream));
   return TL_OK;
 }
 int prof_end(tl_ctx* c, int id, int count) {
   if (!c->prof) return TL_OK;
-  CK(cudaEventRecord(c->qe1, c->stream));
-  CK(cudaEventSynchronize(c->qe1));
-  float ms = 0.f;
-  CK(cudaEventElapsedTime(&ms, c->qe0, c->qe1));
-  c->prof_ms[id] += ms;
-  c->prof_n[id] += count;
+  CK(cudaEventRecord(c->qev[2 * c->qn + 1], c->stream));
+  c->qid[c->qn] = id;
+  c->qcount[c->qn] = count;
+  c->qn += 1;
   return TL_OK;
 }
 
@@ -267,6 +296,19 @@ bool use_mixed_presteps() {
 bool use_fused_ppcg() {
   const char* e = getenv("TL_PPCG_FUSED");
   return !(e && e[0] == '0');
+}
+
+// TL_SETUP_CACHE=0: rebuild Kx, Ky, Di (and the preconditioner set-up) in every solve even when
+// density and dt are those of the previous solve (same results; for checking the cache).
+bool use_setup_cache() {
+  const char* e = getenv("TL_SETUP_CACHE");
+  return !(e && e[0] == '0');
+}
+
+// Fields whose upload (or halo update) changes an input of the set-up cache.
+bool writes_setup_input(int field) {
+  return field == TL_FIELD_DENSITY || field == TL_FIELD_KX || field == TL_FIELD_KY || field == TL_FIELD_DI ||
+         field == TL_FIELD_MI;
 }
 
 // The persistent CG kernel replaces the batched kernels up to this many cells (plain or
@@ -468,8 +510,7 @@ int tl_create(int x_cells, int y_cells, int halo_depth, int coefficient, int pre
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
   for (int i = 0; i < 3 * tl_ctx::BATCH && e == cudaSuccess; ++i) e = cudaEventCreate(&c->pev[i]);
-  if (e == cudaSuccess) e = cudaEventCreate(&c->qe0);
-  if (e == cudaSuccess) e = cudaEventCreate(&c->qe1);
+  for (int i = 0; i < 2 * tl_ctx::QCAP && e == cudaSuccess; ++i) e = cudaEventCreate(&c->qev[i]);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e == cudaSuccess) cg_w_slots();  // occupancy of the matvec sweep, queried outside any capture
   if (e != cudaSuccess) {
@@ -531,8 +572,8 @@ int tl_destroy(tl_ctx* c) {
   if (c->ev1) cudaEventDestroy(c->ev1);
   for (int i = 0; i < 3 * tl_ctx::BATCH; ++i)
     if (c->pev[i]) cudaEventDestroy(c->pev[i]);
-  if (c->qe0) cudaEventDestroy(c->qe0);
-  if (c->qe1) cudaEventDestroy(c->qe1);
+  for (int i = 0; i < 2 * tl_ctx::QCAP; ++i)
+    if (c->qev[i]) cudaEventDestroy(c->qev[i]);
   if (c->up) cudaStreamSynchronize(c->up);
   if (c->down) cudaStreamSynchronize(c->down);
   cudaFree(c->xfer);
@@ -621,6 +662,7 @@ int tl_upload_field(tl_ctx* c, int field, const double* host, int ld) {
   double* d = field_ptr(c, field);
   if (!d) return fail(TL_ERR_ARG, "tl_upload_field: unknown field id");
   if (ld < c->L.nx) return fail(TL_ERR_ARG, "tl_upload_field: ld < x_cells");
+  if (writes_setup_input(field)) c->setup_valid = false;
   if (span_fits(c, ld) && staging(c)) {
     CK(cudaMemcpyAsync(c->xfield(5), host, sizeof(double) * host_span(c->L, ld), cudaMemcpyHostToDevice,
                        c->stream));
@@ -659,6 +701,7 @@ int tl_download_field(tl_ctx* c, int field, double* host, int ld) {
 int tl_upload_state(tl_ctx* c, const double* density, const double* energy1, int ld) {
   if (!c || !density || !energy1) return fail(TL_ERR_ARG, "tl_upload_state: null argument");
   if (ld < c->L.nx) return fail(TL_ERR_ARG, "tl_upload_state: ld < x_cells");
+  c->setup_valid = false;
   // Work fields need no clearing: every solve initialises what it reads, and halo cells stay
   // finite (zero from tl_create, or the generator's / reflective copies).
   if (span_fits(c, ld) && staging(c)) {
@@ -716,6 +759,7 @@ int tl_take_staged(tl_ctx* c) {
   if (!c) return fail(TL_ERR_ARG, "tl_take_staged: null context");
   if (c->st_count == 0) return fail(TL_ERR_STATE, "tl_take_staged: no state is staged");
   const int slot = (c->st_head + c->st_count) & 1;  // the oldest
+  c->setup_valid = false;
   CK(cudaStreamWaitEvent(c->stream, c->st_done[slot], 0));
   if (c->st_ld[slot]) {
     launch_unpack(c->f.density, c->xfield(2 * slot), c->st_ld[slot], c->L, c->stream);
@@ -799,6 +843,7 @@ int tl_generate_chunk(tl_ctx* c, int nstates, const double* density, const doubl
     CK(cudaMalloc(&c->states_dev, st.size() * sizeof(double)));
     c->states_cap = nstates;
   }
+  c->setup_valid = false;
   CK(cudaMemsetAsync(c->slab, 0, c->slab_bytes, c->stream));
   CK(cudaMemcpyAsync(c->states_dev, st.data(), st.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   launch_generate(c->f, c->L, nstates, c->states_dev, domain_xmin, domain_ymin, c->g.dx, c->g.dy, c->stream);
@@ -836,6 +881,8 @@ int tl_common_init(tl_ctx* c, double dt) {
   launch_init_cells(c->f, c->L, c->g, true, c->stream);
   int rc = check_launch("common_init");
   if (rc) return rc;
+  c->setup_valid = true;
+  c->setup_dt = dt;
   CK(cudaStreamSynchronize(c->stream));
   return TL_OK;
 }
@@ -997,6 +1044,8 @@ int tl_jacobi_solve(tl_ctx* c, double* error) {
 int tl_update_halo(tl_ctx* c, int field_mask, int depth) {
   if (!c) return fail(TL_ERR_ARG, "tl_update_halo: null context");
   if (depth < 1) return fail(TL_ERR_ARG, "tl_update_halo: depth must be >= 1");
+  for (int id = 1; id <= TL_FIELD_DI; ++id)
+    if ((field_mask & (1 << id)) && writes_setup_input(id)) c->setup_valid = false;
   int rc = do_halo(c, field_mask, depth);
   if (rc) return rc;
   CK(cudaStreamSynchronize(c->stream));
@@ -1032,6 +1081,8 @@ int tl_cheby_coefficients(double eigmin, double eigmax, int n, double* ch_alphas
 
 int tl_profile(tl_ctx* c, int enable) {
   if (!c) return fail(TL_ERR_ARG, "tl_profile: null context");
+  int rc = prof_flush(c);
+  if (rc) return rc;
   c->prof = enable != 0;
   if (c->prof)
     for (int i = 0; i < TL_NUM_KERNEL_TIMERS; ++i) {
@@ -1044,6 +1095,8 @@ int tl_profile(tl_ctx* c, int enable) {
 int tl_profile_read(tl_ctx* c, int kernel_id, double* total_ms, long long* launches) {
   if (!c || !total_ms || !launches) return fail(TL_ERR_ARG, "tl_profile_read: null argument");
   if (kernel_id < 0 || kernel_id >= TL_NUM_KERNEL_TIMERS) return fail(TL_ERR_ARG, "tl_profile_read: bad kernel id");
+  int rc = prof_flush(c);
+  if (rc) return rc;
   *total_ms = c->prof_ms[kernel_id];
   *launches = c->prof_n[kernel_id];
   return TL_OK;
@@ -1259,6 +1312,7 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
   if ((rc = check_launch("finalise"))) return rc;
   CK(cudaEventRecord(c->ev1, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  if ((rc = prof_flush(c))) return rc;
   float ms = 0.f;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
   info->n_exit = inner_total;
@@ -1463,8 +1517,14 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
   if ((rc = do_halo(c, M(TL_FIELD_ENERGY1) | M(TL_FIELD_DENSITY), c->halo_depth))) return rc;
   c->g.rx = dt / (c->g.dx * c->g.dx);
   c->g.ry = dt / (c->g.dy * c->g.dy);
-  launch_init_faces(c->f, c->L, c->g, c->stream);
-  launch_init_cells(c->f, c->L, c->g, false, c->stream);
+  if (c->setup_valid && c->setup_dt == dt && use_setup_cache()) {
+    launch_init_state(c->f, c->L, c->stream);  // u = u0 = energy1*density; the rest is unchanged
+  } else {
+    launch_init_faces(c->f, c->L, c->g, c->stream);
+    launch_init_cells(c->f, c->L, c->g, false, c->stream);
+    c->setup_valid = true;
+    c->setup_dt = dt;
+  }
   if (rhs) {
     launch_copy_interior(c->f.u0, rhs, c->L, c->stream);
     launch_copy_interior(c->f.u, rhs, c->L, c->stream);

@@ -116,6 +116,19 @@ __global__ void k_init_cells(Fields f, Layout L, Geometry g) {
   }
 }
 
+// common_kernel.f90:67-72 alone (u = u0 = energy*density): the set-up of a solve whose face
+// coefficients, Di and preconditioner factors are still those of the previous solve (same
+// density, same dt), so k_init_faces / the rest of k_init_cells would rewrite the same bits.
+__global__ void k_init_state(Fields f, Layout L) {
+  FOR_ROWS(L) {
+    if (j > L.nx) continue;
+    const long long c = L.at(j, k);
+    const double u = __dmul_rn(f.energy1[c], f.density[c]);
+    f.u[c] = u;
+    f.u0[c] = u;
+  }
+}
+
 __global__ void k_init_residual(Fields f, Layout L) {
   FOR_ROWS(L) {
     if (j > L.nx) continue;
@@ -513,6 +526,9 @@ void launch_init_cells(const Fields& f, const Layout& L, const Geometry& g, bool
   { ++launch_counter(); k_init_cells<<<row_grid(L, false), TB, 0, s>>>(f, L, g); }
   if (g.precond == 3) launch_block_init(f, L, g, s);
   if (with_residual) { ++launch_counter(); k_init_residual<<<row_grid(L, false), TB, 0, s>>>(f, L); }
+}
+void launch_init_state(const Fields& f, const Layout& L, cudaStream_t s) {
+  { ++launch_counter(); k_init_state<<<row_grid(L, false), TB, 0, s>>>(f, L); }
 }
 void launch_block_init(const Fields& f, const Layout& L, const Geometry& g, cudaStream_t s) {
   dim3 grid((L.nx + TB - 1) / TB, (L.ny + 3) / 4);

@@ -26,6 +26,7 @@ void set_last_error(const std::string& msg);
 // ---- set-up, summary, generation, halo ----------------------------------
 void launch_init_faces(const Fields& f, const Layout& L, const Geometry& g, cudaStream_t s);
 void launch_init_cells(const Fields& f, const Layout& L, const Geometry& g, bool with_residual, cudaStream_t s);
+void launch_init_state(const Fields& f, const Layout& L, cudaStream_t s);
 void launch_block_init(const Fields& f, const Layout& L, const Geometry& g, cudaStream_t s);
 void launch_generate(const Fields& f, const Layout& L, int nstates, const double* states /*device, 8*nstates*/,
                      double xmin, double ymin, double dx, double dy, cudaStream_t s);

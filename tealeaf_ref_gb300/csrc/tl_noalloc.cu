@@ -12,15 +12,22 @@
 // lives in g_noalloc_scratch, a file-scope __device__ array of NOALLOC_MAX_ROWS + 32
 // doubles (about 128 KiB) that every GPU loading this library holds until the process
 // exits.  Host code must not pass the symbol itself to a kernel (on the host it is only a
-// stand-in, not a device address): the device address is looked up with
-// cudaGetSymbolAddress once per device, on the first call made while that device is
-// current, and cached.
+// stand-in, not a device address): every call looks up the device address with
+// cudaGetSymbolAddress for the device current at the call.  The first call on a device
+// also loads this library's device code there (set-up); make that first call before any
+// stream capture.  Looking the address up on every call, rather than caching it, keeps it
+// right after the caller resets the device or its primary context (cudaDeviceReset, or a
+// reset made by an OpenACC runtime), which can place the array at a new address.
 //
 // Each call overwrites every partial it reads, so nothing has to be cleared between
 // calls; the array keeps the last call's values afterwards.  Calls whose kernels overlap
 // on the GPU (different streams or host threads at the same time) share the one array and
 // race: serialise them.
-#include <mutex>
+//
+// Ordering: the two kernels and the copy of pw run on the legacy default stream, which
+// waits for work on the caller's blocking streams but not for work on streams created with
+// cudaStreamNonBlocking (OpenACC async queues, some framework streams).  The caller must
+// finish its own writes of p, Kx, Ky and Di on such streams before the call.
 #include <string>
 
 #include "../../include/tealeaf_gb300.h"
@@ -33,34 +40,16 @@ namespace {
 
 constexpr int NOALLOC_MAX_ROWS = 16384;  // largest y_cells the scratch array serves
 constexpr int NOALLOC_THREADS = 256;
-constexpr int MAX_DEVICES = 64;
 
 static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_MAX_ROWS + 32];
-
-std::mutex g_mu;
-double* g_scratch[MAX_DEVICES] = {};
 
 int fail(int code, const std::string& msg) {
   tl::set_last_error(msg);
   return code;
 }
 
-// Device address of g_noalloc_scratch for the current device (looked up once per device).
-int scratch_on_current_device(double** out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail(TL_ERR_CUDA, std::string("tl_cg_calc_w_noalloc: ") + cudaGetErrorString(e));
-  if (dev < 0 || dev >= MAX_DEVICES) return fail(TL_ERR_ARG, "tl_cg_calc_w_noalloc: device index out of range");
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return fail(TL_ERR_CUDA, std::string("tl_cg_calc_w_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_scratch[dev] = static_cast<double*>(p);
-  }
-  *out = g_scratch[dev];
-  return TL_OK;
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(TL_ERR_CUDA, std::string("tl_cg_calc_w_noalloc: ") + where + ": " + cudaGetErrorString(e));
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -85,7 +74,7 @@ __device__ double block_sum(double v) {
 __global__ void k_calc_w_rows(int nx, int ny, int h, const double* __restrict__ p, double* __restrict__ w,
                               const double* __restrict__ kx, const double* __restrict__ ky,
                               const double* __restrict__ di, double rx, double ry, double* __restrict__ scratch) {
-  const long long ldx = nx + 2 * h;
+  const long long ldx = (long long)nx + 2LL * h;
   for (int k = blockIdx.x + 1; k <= ny; k += gridDim.x) {
     double acc = 0.0;
     for (int j = threadIdx.x + 1; j <= nx; j += blockDim.x) {
@@ -118,16 +107,28 @@ extern "C" int tl_cg_calc_w_noalloc(int x_cells, int y_cells, int halo_depth, co
     return fail(TL_ERR_ARG, "tl_cg_calc_w_noalloc: x_cells, y_cells and halo_depth must be >= 1");
   if (y_cells > NOALLOC_MAX_ROWS)
     return fail(TL_ERR_ARG, "tl_cg_calc_w_noalloc: y_cells exceeds the 16384-row limit of its fixed scratch array");
-  if ((long long)(x_cells + 2 * halo_depth) * (y_cells + 2 * halo_depth) >= (1LL << 40))
+  const long long dim_x = (long long)x_cells + 2LL * halo_depth, dim_y = (long long)y_cells + 2LL * halo_depth;
+  if (dim_x >= (1LL << 31) || dim_y >= (1LL << 31) || dim_x * dim_y >= (1LL << 40))
     return fail(TL_ERR_ARG, "tl_cg_calc_w_noalloc: array too large");
-  double* scratch = nullptr;
-  int rc = scratch_on_current_device(&scratch);
-  if (rc != TL_OK) return rc;
-  const int grid = y_cells < 4096 ? y_cells : 4096;
-  k_calc_w_rows<<<grid, NOALLOC_THREADS>>>(x_cells, y_cells, halo_depth, p, w, kx, ky, di, rx, ry, scratch);
-  k_sum_rows<<<1, 1024>>>(y_cells, scratch);
-  cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaMemcpy(pw, scratch + NOALLOC_MAX_ROWS, sizeof(double), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return fail(TL_ERR_CUDA, std::string("tl_cg_calc_w_noalloc: ") + cudaGetErrorString(e));
+  // device address of the scratch array on the current device (see the file comment)
+  void* sym = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&sym, g_noalloc_scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress");
+  if (!sym) return fail(TL_ERR_CUDA, "tl_cg_calc_w_noalloc: cudaGetSymbolAddress returned no address");
+  double* scratch = static_cast<double*>(sym);
+  // Launched through cudaLaunchKernel so that each launch's own status is checked; an error
+  // the caller's earlier work left in the runtime's last-error slot is neither reported nor
+  // cleared here.
+  int nx = x_cells, ny = y_cells, h = halo_depth;
+  double rxv = rx, ryv = ry;
+  void* w_args[] = {&nx, &ny, &h, (void*)&p, (void*)&w, (void*)&kx, (void*)&ky, (void*)&di, &rxv, &ryv, &scratch};
+  const unsigned grid = y_cells < 4096 ? (unsigned)y_cells : 4096u;
+  e = cudaLaunchKernel((const void*)k_calc_w_rows, dim3(grid), dim3(NOALLOC_THREADS), w_args, 0, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "launch of the matvec kernel");
+  void* s_args[] = {&ny, &scratch};
+  e = cudaLaunchKernel((const void*)k_sum_rows, dim3(1), dim3(1024), s_args, 0, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "launch of the row-sum kernel");
+  e = cudaMemcpy(pw, scratch + NOALLOC_MAX_ROWS, sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "copy of pw");
   return TL_OK;
 }

@@ -10,16 +10,6 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
-    config.addinivalue_line("markers", "slow: long-running CPU test")
-
-
-def pytest_collection_modifyitems(config, items):
-    if os.environ.get("TL_RUN_SLOW"):
-        return
-    skip = pytest.mark.skip(reason="slow CPU test; set TL_RUN_SLOW=1")
-    for it in items:
-        if "slow" in it.keywords and "gpu" not in it.keywords:
-            it.add_marker(skip)
 
 
 @pytest.fixture(scope="session")

@@ -24,3 +24,21 @@ def test_reference_arm_json_line():
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
     assert "workload" in d["config"]
+
+
+def test_reference_arm_config_equals_gpu_arm():
+    """Both arms print the same config dict for the same arguments; the CPU sample window is
+    reported outside it."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    for solver in ("cg", "ppcg"):
+        argv = ["--impl", "reference", "--solver", solver, "--cells", "128", "--steps", "1", "--warmup", "0",
+                "--iters", "7", "--cpu-iters", "3"]
+        out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py")] + argv, check=True,
+                             capture_output=True, text=True, cwd=ROOT, timeout=600).stdout
+        d = json.loads([ln for ln in out.splitlines() if ln.startswith("{")][0])
+        gpu_args = bench.parse(argv[2:])
+        assert d["config"] == bench.config_json(gpu_args, 1)
+        assert d["metric"] == bench.metric_name(gpu_args)
+        assert d["cpu_sample"]["iterations_per_step"] == 3

@@ -1,0 +1,108 @@
+"""Parity at the full sizes of the synthetic workloads, against the oracle.
+
+The benchmark workloads run at 4096^2 (CG and Jacobi; PPCG and Chebyshev) and 8192^2 (CG),
+all with the reciprocal-density coefficient keyword (tea_leaf_common_kernel.f90:75-101).
+A full time step there takes thousands of iterations, far beyond what the serial oracle
+finishes in a test, so each case solves the first time step of the workload from its
+generated state over a capped iteration window (tl_max_iters), on the GPU and on the oracle,
+and compares (the control flow is tea_solve.f90:37-503):
+
+* the field summary after the step, to 1e-10 relative (field_summary_kernel.f90:44-62),
+* u per cell, to 1e-8 relative (Jacobi: bit for bit -- its update has the reference's bits),
+* the iteration counts, which must be equal (both runs stop at the cap), and the final
+  error variable.
+
+The PPCG and Chebyshev cases hand over from CG after their 20 presteps (tl_ch_cg_epslim is
+set large so that the switch of tea_solve.f90:160-174 happens at the presteps), so the
+eigenvalue estimate, the switch set-up and inner sweeps all run at full size.  These cases
+cover what only the large meshes exercise: the sweeps' row blocking and wave sizing, and
+field slabs above 2^31 bytes.
+
+One more case solves the first time step of a 2048^2 workload to convergence in the
+precision form (FP32 CG steps with FP64 residual replacement) and checks it against the
+oracle's converged FP64 solve (the OpenMP checker build: the serial build's arithmetic per
+cell, global sums over per-thread partials).
+"""
+import numpy as np
+import pytest
+
+from tealeaf_ref_gb300 import deck as dk
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "c2_cg_4096": dict(config=2, solver="cg", max_iters=50),
+    "c2_jacobi_4096": dict(config=2, solver="jacobi", max_iters=50),
+    "c3_ppcg_4096": dict(config=3, solver="ppcg", max_iters=30, ch_cg_presteps=20, ch_cg_epslim=1e30,
+                         ppcg_inner_steps=10),
+    "c3_chebyshev_4096": dict(config=3, solver="chebyshev", max_iters=50, ch_cg_presteps=20, ch_cg_epslim=1e30),
+    "c5_cg_8192": dict(config=5, solver="cg", max_iters=20),
+}
+
+
+def _deck(case):
+    kw = dict(case)
+    d = dk.config_deck(kw.pop("config"), solver=kw.pop("solver"))
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_full_size_window_against_oracle(name):
+    from oracle import oracle
+    from tealeaf_ref_gb300 import native
+
+    d = _deck(CASES[name])
+    dt = d.initial_timestep
+    with native.Chunk.from_deck(d) as c:
+        gi = c.tea_leaf(d)
+        g_sum = c.field_summary()
+        g_u = c.download("u")
+    o = oracle.Chunk.from_deck(d)
+    oi = o.tea_leaf(d, dt)
+    o_sum = o.field_summary()
+    o_u = np.array(o.interior("u"))
+    del o
+
+    assert gi.reported_iterations == oi.reported_iterations == d.max_iters, (gi.reported_iterations,
+                                                                             oi.reported_iterations)
+    if d.solver in ("ppcg", "chebyshev"):
+        assert gi.cg_calc_steps == oi.cg_calc_steps, (gi.cg_calc_steps, oi.cg_calc_steps)
+        assert gi.ppcg_inner_iters == oi.ppcg_inner_iters
+        assert abs(gi.eigmin - oi.eigmin) <= 1e-10 * oi.eigmin and abs(gi.eigmax - oi.eigmax) <= 1e-10 * oi.eigmax
+    if d.solver != "chebyshev":  # Chebyshev refreshes its error only every 10th step past est_itc
+        assert abs(gi.error - oi.error) <= 1e-8 * abs(oi.error), (gi.error, oi.error)
+    s_rel = np.max(np.abs(g_sum - o_sum) / np.abs(o_sum))
+    assert s_rel <= 1e-10, "field summary rel diff %.3e" % s_rel
+    if d.solver == "jacobi":
+        assert np.array_equal(g_u, o_u), "Jacobi u differs from the oracle's bits"
+    else:
+        u_rel = np.max(np.abs(g_u - o_u) / np.abs(o_u))
+        assert u_rel <= 1e-8, "per-cell u rel diff %.3e" % u_rel
+
+
+def test_mixed_cg_converged_2048_against_oracle():
+    """First time step of the 2048^2 workload (8 rectangles, seed 4) solved to tl_eps 1e-15:
+    the precision form against the oracle's FP64 solve, field summary 1e-10, u 1e-8."""
+    from oracle import oracle
+    from tealeaf_ref_gb300 import native
+
+    d = dk.config_deck(4)
+    dt = d.initial_timestep
+    with native.Chunk.from_deck(d) as c:
+        gi = c.tea_leaf(native.opts_from_deck(d, "mixed"), dt)
+        g_sum = c.field_summary()
+        g_u = c.download("u")
+    o = oracle.Chunk.from_deck(d, threaded="par")
+    oi = o.tea_leaf(d, dt)
+    o_sum = o.field_summary()
+    o_u = np.array(o.interior("u"))
+    del o
+    assert oi.reported_iterations < d.max_iters
+    s_rel = np.max(np.abs(g_sum - o_sum) / np.abs(o_sum))
+    u_rel = np.max(np.abs(g_u - o_u) / np.abs(o_u))
+    print("mixed vs oracle at 2048^2: summary %.2e, u %.2e, stop %s" % (
+        s_rel, u_rel, native.STOP_REASONS.get(gi.stop_reason, gi.stop_reason)))
+    assert s_rel <= 1e-10, "field summary rel diff %.3e" % s_rel
+    assert u_rel <= 1e-8, "per-cell u rel diff %.3e" % u_rel

@@ -255,3 +255,61 @@ def test_two_contexts_interleaved_bitwise():
             cb.tea_leaf(ob, db.initial_timestep)
         np.testing.assert_array_equal(ca.download("u"), ua)
         np.testing.assert_array_equal(cb.download("u"), ub)
+
+
+@pytest.mark.parametrize("case", [dict(), dict(precond="jac_diag"), dict(precond="jac_block"), dict(reflective=True),
+                                  dict(solver="jacobi", max_iters=300, eps=1e-10)],
+                         ids=["cg", "jac_diag", "jac_block", "reflective", "jacobi"])
+def test_setup_cache_bitwise(case, monkeypatch):
+    """Kx, Ky, Di and the preconditioner set-up are rebuilt only when density or dt changed
+    since the last solve: the cached run gives the bits of a run that rebuilds them every time
+    step (TL_SETUP_CACHE=0), as the reference's tea_leaf_common_init does."""
+    from tealeaf_ref_gb300 import native
+
+    kw = dict(nx=203, ny=151, steps=3, n_rect=4, n_circ=2, max_iters=20000)
+    kw.update(case)
+    d = small_deck(**kw)
+    runs = []
+    for cache in ("1", "0"):
+        monkeypatch.setenv("TL_SETUP_CACHE", cache)
+        with native.Chunk.from_deck(d) as c:
+            its = [c.tea_leaf(d).reported_iterations for _ in range(d.end_step)]
+            runs.append((c.field_summary(), c.download("u"), c.download("kx"), its))
+    for a, b in zip(runs[0], runs[1]):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_setup_cache_follows_density_and_dt():
+    """A solve after a new density (upload, staged take, field upload) or a new dt rebuilds the
+    set-up: each result equals a fresh context's on the same state, bit for bit."""
+    from tealeaf_ref_gb300 import native
+
+    d = small_deck(nx=130, ny=97, steps=1, n_rect=3, n_circ=1, max_iters=20000)
+    with native.Chunk.from_deck(d) as c:
+        dens, ener = c.download("density"), c.download("energy1")
+    dens2 = dens * (1.0 + 0.25 * np.sin(np.arange(dens.size)).reshape(dens.shape))
+    dt, dt2 = d.initial_timestep, 0.5 * d.initial_timestep
+
+    def fresh(density, energy, step_dt):
+        with native.Chunk.from_deck(d) as c:
+            c.upload_state(density, energy)
+            c.tea_leaf(d, step_dt)
+            return c.download("u")
+
+    with native.Chunk.from_deck(d) as c:
+        c.tea_leaf(d, dt)
+        c.upload_state(dens2, ener)
+        c.tea_leaf(d, dt)
+        np.testing.assert_array_equal(c.download("u"), fresh(dens2, ener, dt))
+        c.upload_state(dens2, ener)
+        c.tea_leaf(d, dt2)
+        np.testing.assert_array_equal(c.download("u"), fresh(dens2, ener, dt2))
+        c.upload("density", dens)
+        c.upload("energy1", ener)
+        c.tea_leaf(d, dt2)
+        np.testing.assert_array_equal(c.download("u"), fresh(dens, ener, dt2))
+        c.stage_state(dens2, ener)
+        c.take_staged()
+        c.tea_leaf(d, dt2)
+        np.testing.assert_array_equal(c.download("u"), fresh(dens2, ener, dt2))
+        c.wait_transfers()

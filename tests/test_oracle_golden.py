@@ -37,13 +37,11 @@ def test_benchmark_exact(golden, name):
     _check_exact(g, res)
 
 
-@pytest.mark.slow
 def test_benchmark_exact_1000(golden):
     g, res = _run(golden, "tea_bm_4")
     _check_exact(g, res)
 
 
-@pytest.mark.slow
 def test_ppcg_deck_qa(golden):
     d = dk.parse_deck(golden["ppcg_deck"])
     assert d.solver == "ppcg" and d.halo_depth == 2 and d.effective_inner_steps() == 124

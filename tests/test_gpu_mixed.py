@@ -168,3 +168,33 @@ def test_blocked_poly_sweeps_bitwise(solver, reflective, monkeypatch):
     for u, its in runs[1:]:
         assert its == runs[0][1]
         np.testing.assert_array_equal(u, runs[0][0])
+
+
+@pytest.mark.parametrize("solver", ["ppcg", "chebyshev"])
+def test_blocked_sweep_wait_is_bounded(solver, monkeypatch):
+    """The blocked FP32 polynomial sweep's waits for staged rows end by themselves: with one
+    row's mbarrier armed and its tensor copies never issued (TL_POLY_TEST_HOLD=1), the waiting
+    warp gives up after a bounded number of polls, waits (bounded) for its other copies in
+    flight and returns; the later sweeps of the solve return at once, the solve reports
+    TL_ERR_TIMEOUT, and the same context then solves normally."""
+    import time
+
+    from tealeaf_ref_gb300 import native
+
+    d = small_deck(nx=300, ny=160, steps=1, n_rect=4, n_circ=2, max_iters=20000, solver=solver,
+                   ch_cg_presteps=20, ppcg_inner_steps=10)
+    opts = native.opts_from_deck(d, precision="mixed")
+    monkeypatch.delenv("TL_POLY_TMA", raising=False)
+    monkeypatch.delenv("TL_POLY_STEPS_PER_SWEEP", raising=False)
+    with native.Chunk.from_deck(d) as c:
+        monkeypatch.setenv("TL_POLY_TEST_HOLD", "1")
+        t0 = time.perf_counter()
+        with pytest.raises(native.TeaLeafError) as e:
+            c.tea_leaf(opts, d.initial_timestep)
+        assert e.value.code == -5  # TL_ERR_TIMEOUT
+        assert time.perf_counter() - t0 < 60
+        monkeypatch.delenv("TL_POLY_TEST_HOLD")
+        c.generate(d)
+        c.reset_eigen()
+        info = c.tea_leaf(opts, d.initial_timestep)
+        assert info.reported_iterations > 0

@@ -72,3 +72,17 @@ def test_oracle_reflective_and_jacobi_quirk():
     r = c.array("r")
     h = c.h
     assert np.all(r[:h, :] == 0.0) and np.all(r[:, :h] == 0.0)
+
+
+def test_exact_summary_helper_matches_serial_summary():
+    """The correctly rounded field summary the full-size parity tests use agrees with the
+    oracle's serial field_summary where the serial sums' rounding is negligible (small meshes)."""
+    import sys
+    import os
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from helpers import exact_summary, small_deck
+
+    d = small_deck(nx=120, ny=77, steps=1)
+    o = oracle.Chunk.from_deck(d)
+    o.tea_leaf(d)
+    np.testing.assert_allclose(exact_summary(o), o.field_summary(), rtol=1e-13)

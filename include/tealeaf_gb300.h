@@ -161,6 +161,15 @@ int tl_device_bytes(const tl_ctx* ctx, unsigned long long* bytes);
  * speed without staging -- e.g. the Fortran driver's density/energy1 arrays.  bytes > 0. */
 int tl_host_register(void* host, unsigned long long bytes);
 int tl_host_unregister(void* host);
+/* Allocate / free page-locked host memory from the CUDA driver (cudaHostAlloc), for host
+ * arrays that cross the boundary every time step.  On a Grace host (64 KB base pages), copies
+ * from memory registered with tl_host_register stall a solve running at the same time
+ * (measured: a 100-iteration 8192^2 CG solve took 317 ms instead of 135 ms under a concurrent
+ * 1.6 GB upload), and copies made between solves run at a few GB/s; memory from
+ * tl_host_alloc copies at ~200 GB/s and slows a concurrent solve by ~5%.  A Fortran driver
+ * maps it with C_F_POINTER. */
+int tl_host_alloc(unsigned long long bytes, void** host);
+int tl_host_free(void* host);
 
 /* Host <-> device copies of one field's interior (x_cells x y_cells, leading dimension ld).
  * The host array moves as one contiguous copy and is unpacked / packed on the device (the
@@ -213,6 +222,10 @@ int tl_calc_residual(tl_ctx* ctx);
 int tl_calc_2norm(tl_ctx* ctx, int norm_array, double* norm);
 /* tea_leaf_kernel_finalise (common_kernel.f90:179-206): energy1 = u/density. */
 int tl_finalise(tl_ctx* ctx);
+/* tea_leaf_kernel_finalise followed by field_summary_kernel (field_summary_kernel.f90:26-64),
+ * in one sweep: energy1 = u/density, then vol, mass, ie, temp of the new state -- the same
+ * values (bit for bit) as tl_finalise + tl_field_summary. */
+int tl_finalise_field_summary(tl_ctx* ctx, double* vol, double* mass, double* ie, double* temp);
 /* tea_leaf_cg_init_kernel (kernels/tea_leaf_cg_kernel.f90:31-112): p = r (or M^-1 r), rro = r.p. */
 int tl_cg_init(tl_ctx* ctx, double* rro);
 /* tea_leaf_cg_calc_w_kernel (cg_kernel.f90:114-156): w = A p, pw = p.w. */
@@ -272,6 +285,10 @@ int tl_cg_calc_w_noalloc(int x_cells, int y_cells, int halo_depth, const double*
  * of iterations.  Eigenvalue estimates persist in the context across calls, as the
  * reference's SAVE variables do. */
 int tl_tea_leaf(tl_ctx* ctx, const tl_solve_opts* opts, double dt, tl_solve_info* info);
+/* tl_tea_leaf for a time step after which the driver calls field_summary (diffuse.f90:58-61,
+ * field_summary.f90:27-101): the solve's finalise sweep also forms the summary; summary[0..3] =
+ * vol, mass, ie, temp, bit for bit those of tl_field_summary after tl_tea_leaf. */
+int tl_tea_leaf_summary(tl_ctx* ctx, const tl_solve_opts* opts, double dt, tl_solve_info* info, double* summary);
 /* Forget the saved eigenvalue estimates (the reference's 'first' flag becomes true). */
 int tl_reset_eigen(tl_ctx* ctx);
 

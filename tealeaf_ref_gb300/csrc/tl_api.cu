@@ -78,6 +78,8 @@ struct tl_ctx {
   // tea_leaf_common_init would produce different values.
   bool setup_valid = false;
   double setup_dt = 0.0;
+  // tl_tea_leaf_summary: the solve's finalise sweep also forms the field summary (st->red)
+  bool want_summary = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // per-launch timers of the fused loop kernels (tl_profile)
   static constexpr int BATCH = 16;
@@ -92,6 +94,12 @@ struct tl_ctx {
   // CUDA graphs of one batch of the device-resident loops (captured once per set of kernel
   // arguments): the fused CG batch and the mixed-precision CG batch
   cudaGraphExec_t cg_exec = nullptr, mix_exec = nullptr;
+  // the fused CG batch with events recorded around the two kernels of its second iteration
+  // (tl_profile on): one sampled iteration per batch, so the events (graph nodes) hardly
+  // perturb the timed launches
+  cudaGraphExec_t cg_prof_exec = nullptr;
+  LoopArgs cg_prof_key{};
+  long long cg_prof_nk = 0;
   int pgrid = -1;  // co-resident CTAs of the persistent CG kernel (-1: not yet queried)
   // host transfers: an upload and a download stream (tl_stage_state, tl_fetch_field) and
   // XFER_FIELDS staging fields -- two staged (density, energy1) pairs, the fetch snapshot, and
@@ -298,6 +306,18 @@ bool use_fused_ppcg() {
   return !(e && e[0] == '0');
 }
 
+// The last sweep of a solve: energy1 = u / density (tea_leaf_kernel_finalise), with the CG
+// loop's pending deferred u update applied first when `flush`, and fused with the field summary
+// when the caller asked for one (tl_tea_leaf_summary).
+void finalise_sweep(tl_ctx* c, bool flush) {
+  if (c->want_summary)
+    launch_finalise_summary(c->f, c->L, c->g.dx * c->g.dy, c->rd(), flush ? c->st : nullptr, c->stream);
+  else if (flush)
+    launch_finalise_flush(c->f, c->L, c->st, c->stream);
+  else
+    launch_finalise(c->f, c->L, c->stream);
+}
+
 // TL_SETUP_CACHE=0: rebuild Kx, Ky, Di (and the preconditioner set-up) in every solve even when
 // density and dt are those of the previous solve (same results; for checking the cache).
 bool use_setup_cache() {
@@ -341,6 +361,36 @@ int run_cg_batch(tl_ctx* c, const LoopArgs& la) {
   }
   CK(cudaGraphLaunch(c->cg_exec, c->stream));
   launch_counter() += c->cg_nk;
+  return TL_OK;
+}
+
+// The same batch with the per-kernel timer events of its sampled iteration TIMED_ITER recorded
+// as graph nodes: pev[0] before that iteration's matvec sweep, pev[1] between the sweeps, pev[2]
+// after the update sweep.
+constexpr int TIMED_ITER = 1;
+int run_cg_batch_timed(tl_ctx* c, const LoopArgs& la) {
+  if (!c->cg_prof_exec || !same_loop_args(c->cg_prof_key, la)) {
+    cudaError_t rec = cudaSuccess;
+    int rc = capture_batch(c, &c->cg_prof_exec, &c->cg_prof_nk, [&] {
+      for (int i = 0; i < tl_ctx::BATCH; ++i) {
+        const bool t = i == TIMED_ITER;
+        if (t && rec == cudaSuccess) rec = cudaEventRecordWithFlags(c->pev[0], c->stream, cudaEventRecordExternal);
+        launch_fused_cg_w(la, false, c->stream);
+        if (t && rec == cudaSuccess) rec = cudaEventRecordWithFlags(c->pev[1], c->stream, cudaEventRecordExternal);
+        launch_fused_cg_ur(la, c->stream);
+        if (t && rec == cudaSuccess) rec = cudaEventRecordWithFlags(c->pev[2], c->stream, cudaEventRecordExternal);
+      }
+    });
+    if (rc) return rc;
+    if (rec != cudaSuccess) {
+      cudaGraphExecDestroy(c->cg_prof_exec);
+      c->cg_prof_exec = nullptr;
+      return cuda_fail(rec, "cudaEventRecordWithFlags (capture)");
+    }
+    c->cg_prof_key = la;
+  }
+  CK(cudaGraphLaunch(c->cg_prof_exec, c->stream));
+  launch_counter() += c->cg_prof_nk;
   return TL_OK;
 }
 
@@ -586,6 +636,7 @@ int tl_destroy(tl_ctx* c) {
   if (c->up) cudaStreamDestroy(c->up);
   if (c->down) cudaStreamDestroy(c->down);
   if (c->cg_exec) cudaGraphExecDestroy(c->cg_exec);
+  if (c->cg_prof_exec) cudaGraphExecDestroy(c->cg_prof_exec);
   if (c->mix_exec) cudaGraphExecDestroy(c->mix_exec);
   cudaFree(c->tape);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -602,6 +653,25 @@ int tl_host_register(void* host, unsigned long long bytes) {
 int tl_host_unregister(void* host) {
   if (!host) return fail(TL_ERR_ARG, "tl_host_unregister: null pointer");
   CK(cudaHostUnregister(host));
+  return TL_OK;
+}
+
+int tl_host_alloc(unsigned long long bytes, void** host) {
+  if (!host || bytes == 0) return fail(TL_ERR_ARG, "tl_host_alloc: null pointer or zero size");
+  *host = nullptr;
+  const cudaError_t e = cudaHostAlloc(host, (size_t)bytes, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    *host = nullptr;
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? fail(TL_ERR_ALLOC, "tl_host_alloc: cudaHostAlloc failed")
+                                          : cuda_fail(e, "tl_host_alloc");
+  }
+  return TL_OK;
+}
+
+int tl_host_free(void* host) {
+  if (!host) return fail(TL_ERR_ARG, "tl_host_free: null pointer");
+  CK(cudaFreeHost(host));
   return TL_OK;
 }
 
@@ -1118,7 +1188,7 @@ int ensure_mix(tl_ctx* c) {
   float* b = reinterpret_cast<float*>(c->mix_slab);
   const size_t step = fb / sizeof(float);
   c->mix = MixFields{b,            b + step,     b + 2 * step, b + 3 * step, b + 4 * step,
-                     b + 5 * step, b + 6 * step, b + 7 * step, b + 8 * step, c->counter + 8};
+                     b + 5 * step, b + 6 * step, b + 7 * step, b + 8 * step, c->counter + MIX_ERR_WORD};
   CK(cudaMalloc(&c->mst, sizeof(MixState)));
   CK(cudaMallocHost(&c->mst_host, sizeof(MixState)));
   if (prepare_mix_kernels() != 0) return fail(TL_ERR_CUDA, "cannot set the mixed-precision kernels' shared memory");
@@ -1129,6 +1199,19 @@ int sync_mix(tl_ctx* c) {
   CK(cudaMemcpyAsync(c->mst_host, c->mst, sizeof(MixState), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return TL_OK;
+}
+
+// TL_ERR_TIMEOUT (the word cleared) if a blocked FP32 sweep set the error word: a staged row did
+// not arrive within its bounded wait (1), or its shared memory was misaligned for TMA (2).
+int check_mix_err(tl_ctx* c) {
+  unsigned werr = 0;
+  CK(cudaMemcpyAsync(&werr, c->mix.err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (!werr) return TL_OK;
+  CK(cudaMemsetAsync(c->mix.err, 0, sizeof(unsigned), c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return fail(TL_ERR_TIMEOUT, werr == 1 ? "tl_tea_leaf: a staged row of a blocked FP32 sweep did not arrive in time"
+                                        : "tl_tea_leaf: shared memory misaligned for the blocked FP32 sweep");
 }
 
 // Starts a fresh FP32 CG process on the correction (d must be zero): r = p = u0 - A u.
@@ -1307,7 +1390,7 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
   }
   if (res < o->eps * initial_residual) stop = TL_STOP_EPS;
   const int inner_total = H.n - 1;
-  launch_finalise(c->f, c->L, c->stream);
+  finalise_sweep(c, false);
   if ((rc = do_halo(c, M(TL_FIELD_ENERGY1), 1))) return rc;
   if ((rc = check_launch("finalise"))) return rc;
   CK(cudaEventRecord(c->ev1, c->stream));
@@ -1395,6 +1478,7 @@ struct Solver {
       launch_mix_trial(c->f, c->mix, c->L, rd, c->mst, false, c->stream, false);  // m.r = u0 - A (u + d)
       if ((rc = check_launch("mixed chebyshev cycle"))) return rc;
       if ((rc = sync_mix(c))) return rc;
+      if ((rc = check_mix_err(c))) return rc;
       total += len;
       const double res_t = std::sqrt(std::fabs(H.trial_rr));
       if (!std::isfinite(res_t)) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite residual");
@@ -1472,7 +1556,16 @@ struct Solver {
       if ((rc = sync_state(c))) return rc;
       *outer_done += 1;
       *inner_done += inner;
-      if (H.status == EXIT_BREAKDOWN) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite PPCG scalar");
+      if (H.status == EXIT_BREAKDOWN) {
+        // a blocked FP32 inner sweep that gave up waiting leaves void values behind, which can
+        // break the outer iteration down before the rrn sweep reports the timeout
+        if (mixed && (rc = check_mix_err(c))) return rc;
+        return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite PPCG scalar");
+      }
+      if (H.status == EXIT_TIMEOUT) {
+        const int e = check_mix_err(c);
+        return e ? e : fail(TL_ERR_TIMEOUT, "tl_tea_leaf: a blocked FP32 sweep gave up waiting");
+      }
       if (H.status != RUN) break;
     }
     *error = H.error;
@@ -1550,12 +1643,16 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
   H.status = RUN;
   H.theta = c->theta;
   if ((rc = push_state(c))) return rc;
-  {
+  const bool cg_family = S.use_cg || S.use_cheby || S.use_ppcg;
+  if (cg_family && c->g.precond != TL_PREC_JAC_BLOCK) {
+    // calc_residual, its 2-norm and cg_init in one sweep
+    launch_residual_cg_init(c->f, c->L, c->g, c->rd(), c->stream);
+  } else {
     Reduce rd = c->rd();
     launch_residual(c->f, c->L, &rd, RED_INIT_RESIDUAL, c->stream);
   }
-  if (S.use_cg || S.use_cheby || S.use_ppcg) {
-    launch_cg_init(c->f, c->L, c->g, c->rd(), RED_RRO, c->stream);
+  if (cg_family) {
+    if (c->g.precond == TL_PREC_JAC_BLOCK) launch_cg_init(c->f, c->L, c->g, c->rd(), RED_RRO, c->stream);
     if ((rc = do_halo(c, M(TL_FIELD_U) | M(TL_FIELD_P), 1))) return rc;
   } else if (S.use_jacobi) {
     launch_jacobi_denominator(c->f, c->L, c->g, c->stream);
@@ -1571,6 +1668,7 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
   bool ch_switch_check = false, ppcg_active = false, exited = false;
   int fields_mask = S.use_jacobi ? M(TL_FIELD_U) : M(TL_FIELD_P);
   const int batch = tl_ctx::BATCH;
+  bool flush_in_finalise = false;  // the CG loop's last u update is left to the finalise sweep
 
   // Precision form without reflective boundaries: the CG presteps before the Chebyshev / PPCG
   // switch (tea_solve.f90:160-174) run as the mixed CG -- FP32 steps with FP64 residual
@@ -1607,6 +1705,7 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
       // device-resident CG loop, batches of iterations, one status read per batch
       LoopArgs la = c->loop();
       const int n_before = n;
+      bool sampled = false;  // the timed graph form: only iteration TIMED_ITER of the batch is timed
       if (use_persistent(c)) {
         launch_flush_u(la, c->stream);  // a pending update of the batched kernels (none normally)
         unsigned* bar = c->counter + 4;  // barrier counter, generation, error word
@@ -1618,6 +1717,9 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
         CK(launch_persistent_cg(la, PERSIST_RUN, bar, c->pgrid, c->stream, ex && ex[0] == '1' ? 1 : 0));
       } else if (!c->prof && use_graphs()) {
         if ((rc = run_cg_batch(c, la))) return rc;
+      } else if (use_graphs()) {
+        if ((rc = run_cg_batch_timed(c, la))) return rc;
+        sampled = true;
       } else {
         for (int i = 0; i < batch; ++i) {
           if (c->prof) CK(cudaEventRecord(c->pev[3 * i], c->stream));
@@ -1630,10 +1732,12 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
       if ((rc = check_launch("cg batch"))) return rc;
       if ((rc = sync_state(c))) return rc;
       if (c->prof) {
-        // iterations of this batch that did work (the rest returned on the status word)
+        // iterations of this batch that did work (the rest returned on the status word); the
+        // graph form times its sampled iteration only
         int ran = (H.status == EXIT_CONVERGED || H.status == EXIT_BREAKDOWN) ? H.n_exit - n_before + 1
                                                                                : H.n - n_before;
         ran = std::min(std::max(ran, 0), batch);
+        if (sampled) ran = ran > TIMED_ITER ? 1 : 0;
         for (int i = 0; i < ran; ++i) {
           float a = 0.f, b = 0.f;
           CK(cudaEventElapsedTime(&a, c->pev[3 * i], c->pev[3 * i + 1]));
@@ -1649,9 +1753,14 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
       if (H.status == EXIT_TIMEOUT)
         return fail(TL_ERR_TIMEOUT, "tl_tea_leaf: a grid-barrier wait of the persistent CG kernel expired");
       if (H.status != RUN) {
-        // the CG phase stops here: apply the deferred u += alpha p of its last iteration
-        launch_flush_u(la, c->stream);
-        H.u_pending = 0;
+        // the CG phase stops here: apply the deferred u += alpha p of its last iteration -- in
+        // the finalise sweep when nothing reads u before it (a CG solve without check_result)
+        if (S.use_cg && finalise && !o->check_result) {
+          flush_in_finalise = true;
+        } else {
+          launch_flush_u(la, c->stream);
+          H.u_pending = 0;
+        }
       }
       error = H.error;
       old_error = H.old_error;
@@ -1746,6 +1855,7 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
         launch_ppcg_init(c->f, c->L, c->g, 3, ppcg_active, c->rd(), RED_STORE, c->stream);
         if ((rc = check_launch("ppcg_init"))) return rc;
         if ((rc = reduce_result(c, &rro))) return rc;
+        if (mixed && (rc = check_mix_err(c))) return rc;  // the set-up's FP32 inner sweeps
         fields_mask = M(TL_FIELD_P);
         if ((rc = do_halo(c, fields_mask, 1))) return rc;
       }
@@ -1846,20 +1956,9 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
     if ((rc = reduce_result(c, &exact_error))) return rc;
     exact_error = std::sqrt(exact_error);
   }
-  if (mixed) {
-    // a blocked FP32 sweep sets this word when a staged row did not arrive within its bounded
-    // wait (1) or its shared memory was misaligned for TMA (2)
-    unsigned werr = 0;
-    CK(cudaMemcpyAsync(&werr, c->mix.err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    if (werr) {
-      CK(cudaMemsetAsync(c->mix.err, 0, sizeof(unsigned), c->stream));
-      return fail(TL_ERR_TIMEOUT, werr == 1 ? "tl_tea_leaf: a staged row of a blocked FP32 sweep did not arrive in time"
-                                            : "tl_tea_leaf: shared memory misaligned for the blocked FP32 sweep");
-    }
-  }
+  if (mixed && (rc = check_mix_err(c))) return rc;
   if (finalise) {
-    launch_finalise(c->f, c->L, c->stream);
+    finalise_sweep(c, flush_in_finalise);
     if ((rc = do_halo(c, M(TL_FIELD_ENERGY1), 1))) return rc;
   }
   if ((rc = check_launch("finalise"))) return rc;
@@ -1892,6 +1991,32 @@ extern "C" int tl_tea_leaf(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solv
   int rc;
   if ((rc = check_opts(c, o))) return rc;
   return solve(c, o, dt, info, nullptr, true);
+}
+
+extern "C" int tl_tea_leaf_summary(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info,
+                                   double* summary) {
+  if (!c || !o || !info || !summary) return fail(TL_ERR_ARG, "tl_tea_leaf_summary: null argument");
+  int rc;
+  if ((rc = check_opts(c, o))) return rc;
+  c->want_summary = true;
+  rc = solve(c, o, dt, info, nullptr, true);
+  c->want_summary = false;
+  if (rc) return rc;
+  return reduce_result(c, summary, 4);
+}
+
+extern "C" int tl_finalise_field_summary(tl_ctx* c, double* vol, double* mass, double* ie, double* temp) {
+  if (!c || !vol || !mass || !ie || !temp) return fail(TL_ERR_ARG, "tl_finalise_field_summary: null argument");
+  launch_finalise_summary(c->f, c->L, c->g.dx * c->g.dy, c->rd(), nullptr, c->stream);
+  int rc = check_launch("finalise_field_summary");
+  if (rc) return rc;
+  double out[4];
+  if ((rc = reduce_result(c, out, 4))) return rc;
+  *vol = out[0];
+  *mass = out[1];
+  *ie = out[2];
+  *temp = out[3];
+  return TL_OK;
 }
 
 // ===========================================================================

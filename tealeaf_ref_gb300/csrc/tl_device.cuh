@@ -90,6 +90,11 @@ struct LoopState {
   double u_alpha;
 };
 
+// Word of the context's counter buffer that a blocked FP32 sweep of the precision form sets
+// when a bounded wait for a staged row expired (1) or its shared memory was misaligned (2):
+// MixFields::err points here, and the PPCG loop's epilogue turns it into EXIT_TIMEOUT.
+constexpr int MIX_ERR_WORD = 8;
+
 // Launch-independent pointers handed to every kernel that reduces.
 struct Reduce {
   double* partials;    // [gridDim.x * gridDim.y][NV]
@@ -107,22 +112,27 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Block sum of NV values in fixed order; result valid in thread 0.  scratch: 32*NV doubles.
+// Largest CTA of a kernel that reduces (block_sum's shared scratch is sized for it).
+constexpr int MAX_REDUCE_THREADS = 256;
+
+// Block sum of NV values in fixed order; result valid in thread 0.  scratch: NV *
+// MAX_REDUCE_THREADS doubles.  Every thread parks its values in shared memory and the first warp
+// adds them (a column sum, then a shuffle tree): blockDim/32 + 4 FP64 additions per value, in
+// one warp.  A shuffle tree in every warp would cost 5 per warp -- FP64 instructions are what
+// the reducing sweeps are short of on this GPU.
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double* scratch) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const int t = threadIdx.x, nt = blockDim.x;
+  __syncthreads();  // an earlier use of scratch in this CTA is complete
 #pragma unroll
-  for (int i = 0; i < NV; ++i) v[i] = warp_sum(v[i]);
+  for (int i = 0; i < NV; ++i) scratch[i * MAX_REDUCE_THREADS + t] = v[i];
   __syncthreads();
-  if (lane == 0) {
-#pragma unroll
-    for (int i = 0; i < NV; ++i) scratch[wid * NV + i] = v[i];
-  }
-  __syncthreads();
-  if (wid == 0) {
+  if (t < 32) {
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
-      double x = lane < nw ? scratch[lane * NV + i] : 0.0;
+      const double* s = scratch + i * MAX_REDUCE_THREADS;
+      double x = t < nt ? s[t] : 0.0;
+      for (int k = t + 32; k < nt; k += 32) x += s[k];
       v[i] = warp_sum(x);
     }
   }
@@ -134,7 +144,7 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* scratch) {
 // depend on which CTA arrives last.
 template <int NV, typename Epi>
 __device__ __forceinline__ void grid_reduce(double (&v)[NV], const Reduce& rd, Epi epi) {
-  __shared__ double scratch[32 * NV];
+  __shared__ double scratch[MAX_REDUCE_THREADS * NV];
   __shared__ int is_last;
   block_sum<NV>(v, scratch);
   const unsigned nblk = gridDim.x * gridDim.y;

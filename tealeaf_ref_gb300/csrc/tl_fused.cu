@@ -58,17 +58,19 @@ __device__ __forceinline__ void finish_iteration(LoopState* st, double err_raw) 
   }
 }
 
+// the matvec sweep's sums: p.w (CG), and z.r (PPCG)
+template <bool PPCG>
 struct EpiCgW {
+  static constexpr int NV = PPCG ? 2 : 1;
   Reduce rd;
-  bool ppcg;
-  __device__ void operator()(double (&acc)[2]) const {
+  __device__ void operator()(double (&acc)[NV]) const {
     LoopState* st = rd.st;
     st->u_pending = 0;  // every CTA applied the deferred u update for its cells
     st->pw = acc[0];
-    if (ppcg) st->rro = acc[1];  // tea_leaf_ppcg_calc_zrnorm, allsum2 (tea_solve.f90:300-303)
+    if constexpr (PPCG) st->rro = acc[1];  // tea_leaf_ppcg_calc_zrnorm, allsum2 (tea_solve.f90:300-303)
     const double alpha = st->rro / st->pw;
     st->alpha = alpha;
-    if (!ppcg) rd.hist_a[st->n] = alpha;
+    if constexpr (!PPCG) rd.hist_a[st->n] = alpha;
     if (!isfinite(alpha)) {
       st->status = EXIT_BREAKDOWN;
       st->n_exit = st->n;
@@ -156,7 +158,7 @@ __global__ void __launch_bounds__(FT) k_fused_cg_w(LoopArgs a, int rows_per_cta)
   const double ua = st->u_alpha;
   double* __restrict__ u = a.f.u;
 
-  double acc[2] = {0.0, 0.0};
+  double acc[EpiCgW<PPCG>::NV] = {};
   double acc_b = 0.0;  // second column's p.w chain, kept separate to shorten the FMA dependency chain
   double2 pm = make_double2(0.0, 0.0), pc = pm, pnx = pm, cyc = pm, oc = pm, onx = pm;
   if (active) {
@@ -215,7 +217,7 @@ __global__ void __launch_bounds__(FT) k_fused_cg_w(LoopArgs a, int rows_per_cta)
         pout[c] = pc.x;
         if (upd_u) u[c] = fma(ua, oc.x, u[c]);
       }
-      if (PPCG) {
+      if constexpr (PPCG) {
         // tea_leaf_ppcg_store_r (ppcg_kernel.f90:507-530) and calc_zrnorm z.r (:411-451)
         const double2 rr = *reinterpret_cast<const double2*>(a.f.r + c);
         const double2 zz = *reinterpret_cast<const double2*>(a.f.z + c);
@@ -233,7 +235,7 @@ __global__ void __launch_bounds__(FT) k_fused_cg_w(LoopArgs a, int rows_per_cta)
     oc = onx;
   }
   acc[0] += acc_b;
-  grid_reduce<2>(acc, a.rd, EpiCgW{a.rd, PPCG});
+  grid_reduce<EpiCgW<PPCG>::NV>(acc, a.rd, EpiCgW<PPCG>{a.rd});
 }
 
 // ---- persistent cooperative CG (small meshes) ----------------------------------------------
@@ -295,7 +297,7 @@ __device__ __forceinline__ double pb_total(const double* partials, int nb, doubl
 // of the bounded wait (an arrival that never comes)
 __global__ void __launch_bounds__(PB_T) k_persistent_cg(LoopArgs a, int max_run, unsigned* bar, int extra_arrivals) {
   __shared__ LoopState S;
-  __shared__ double scratch[32];
+  __shared__ double scratch[MAX_REDUCE_THREADS];
   __shared__ double bcast;
   const Layout L = a.L;
   const unsigned nb = gridDim.x;
@@ -532,6 +534,11 @@ struct EpiPpcgRrn {
     st->p_pending = 1;
     st->rro = rrn;
     finish_iteration(st, rrn);
+    // a blocked FP32 inner sweep of this iteration gave up waiting for a staged row: stop here
+    if (rd.counter[MIX_ERR_WORD] != 0u) {
+      st->status = EXIT_TIMEOUT;
+      st->n_exit = st->n;
+    }
   }
 };
 

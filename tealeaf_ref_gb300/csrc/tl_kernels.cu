@@ -228,16 +228,46 @@ __global__ void k_generate(Fields f, Layout L, int nstates, const double* __rest
 }
 
 // field_summary_kernel.f90:44-62: vol, mass, ie, temp.
+// One cell's terms of the summary, in the order k_finalise_summary adds them too (same grid,
+// same per-thread order: the two kernels give the same bits).
+__device__ __forceinline__ void summary_terms(double (&v)[4], double cell_vol, double rho, double e, double u) {
+  const double cell_mass = cell_vol * rho;
+  v[0] += cell_vol;
+  v[1] += cell_mass;
+  v[2] = fma(cell_mass, e, v[2]);
+  v[3] = fma(cell_mass, u, v[3]);
+}
+
 __global__ void k_field_summary(Fields f, Layout L, double cell_vol, Reduce rd) {
   double v[4] = {0.0, 0.0, 0.0, 0.0};
   FOR_ROWS(L) {
     if (j > L.nx) continue;
     const long long c = L.at(j, k);
-    const double cell_mass = cell_vol * f.density[c];
-    v[0] += cell_vol;
-    v[1] += cell_mass;
-    v[2] += cell_mass * f.energy1[c];
-    v[3] += cell_mass * f.u[c];
+    summary_terms(v, cell_vol, f.density[c], f.energy1[c], f.u[c]);
+  }
+  grid_reduce<4>(v, rd, EpiMode<4>{rd.st, RED_STORE});
+}
+
+// tea_leaf_kernel_finalise (common_kernel.f90:179-206) fused with field_summary_kernel
+// (field_summary_kernel.f90:44-62): energy1 = u / density and vol, mass, ie, temp in one sweep
+// (st->red[0..4)).  st non-null: the CG loop's pending deferred u += alpha p is applied first.
+__global__ void k_finalise_summary(Fields f, Layout L, double cell_vol, Reduce rd, const LoopState* __restrict__ st) {
+  const bool pending = st && st->u_pending != 0;
+  const double ua = pending ? st->u_alpha : 0.0;
+  const double* __restrict__ p = (pending && st->u_psel) ? f.p2 : f.p;
+  double v[4] = {0.0, 0.0, 0.0, 0.0};
+  FOR_ROWS(L) {
+    if (j > L.nx) continue;
+    const long long c = L.at(j, k);
+    double u = f.u[c];
+    if (pending) {
+      u = fma(ua, p[c], u);
+      f.u[c] = u;
+    }
+    const double rho = f.density[c];
+    const double e = u / rho;
+    f.energy1[c] = e;
+    summary_terms(v, cell_vol, rho, e, u);
   }
   grid_reduce<4>(v, rd, EpiMode<4>{rd.st, RED_STORE});
 }
@@ -335,6 +365,60 @@ __global__ void k_finalise(Fields f, Layout L) {
     if (j > L.nx) continue;
     const long long c = L.at(j, k);
     f.energy1[c] = f.u[c] / f.density[c];
+  }
+}
+
+// The start of a CG solve in one sweep: tea_leaf_calc_residual_kernel (common_kernel.f90:208-244,
+// r = u0 - A u), tea_leaf_calc_2norm_kernel of r (:246-274; the initial residual and old_error,
+// tea_solve.f90:124-130) and tea_leaf_cg_init_kernel (cg_kernel.f90:31-112) without a
+// preconditioner (p = r, z = 0, rro = r.p) or with jac_diag (z = Mi r, p = z, rro = r.z).
+struct EpiResidualCgInit {
+  LoopState* st;
+  __device__ void operator()(double (&acc)[2]) const {
+    st->old_error = acc[0];
+    st->initial_residual = sqrt(fabs(acc[0]));
+    st->rro = acc[1];
+    st->red[0] = acc[0];
+    st->red[1] = acc[1];
+  }
+};
+template <bool DIAG>
+__global__ void k_residual_cg_init(Fields f, Layout L, Reduce rd) {
+  double v[2] = {0.0, 0.0};
+  FOR_ROWS(L) {
+    if (j > L.nx) continue;
+    const long long c = L.at(j, k);
+    const double r = f.u0[c] - apply_A(f.u, f.cx, f.cy, f.di, c, L.ld);
+    f.r[c] = r;
+    double p = r;
+    if (DIAG) {
+      p = f.mi[c] * r;
+      f.z[c] = p;
+    } else {
+      f.z[c] = 0.0;
+    }
+    f.p[c] = p;
+    v[0] = fma(r, r, v[0]);
+    v[1] = fma(r, p, v[1]);
+  }
+  grid_reduce<2>(v, rd, EpiResidualCgInit{rd.st});
+}
+
+// tea_leaf_kernel_finalise with the CG loop's last deferred u += alpha p (LoopState::u_pending)
+// applied in the same sweep: u = u + alpha p, energy1 = u / density.
+__global__ void k_finalise_flush(Fields f, Layout L, const LoopState* __restrict__ st) {
+  const bool pending = st->u_pending != 0;
+  const double ua = st->u_alpha;
+  const double* __restrict__ p = st->u_psel ? f.p2 : f.p;
+  FOR_ROWS(L) {
+    if (j > L.nx) continue;
+    const long long c = L.at(j, k);
+    double u = f.u[c];
+    if (pending) {
+      u = fma(ua, p[c], u);
+      f.u[c] = u;
+    }
+    f.energy1[c] = u / f.density[c];
   }
 }
 
@@ -578,6 +662,21 @@ void launch_precond(const Fields& f, const Layout& L, const Geometry& g, const d
   } else if (g.precond == 2) {
     { ++launch_counter(); k_diag_solve<<<row_grid(L, false), TB, 0, s>>>(L, f.mi, src, dst); }
   }
+}
+void launch_residual_cg_init(const Fields& f, const Layout& L, const Geometry& g, const Reduce& rd, cudaStream_t s) {
+  if (g.precond == 2)
+    { ++launch_counter(); k_residual_cg_init<true><<<row_grid(L, true), TB, 0, s>>>(f, L, rd); }
+  else
+    { ++launch_counter(); k_residual_cg_init<false><<<row_grid(L, true), TB, 0, s>>>(f, L, rd); }
+}
+void launch_finalise_summary(const Fields& f, const Layout& L, double cell_vol, const Reduce& rd, LoopState* flush_st,
+                             cudaStream_t s) {
+  { ++launch_counter(); k_finalise_summary<<<row_grid(L, true), TB, 0, s>>>(f, L, cell_vol, rd, flush_st); }
+  if (flush_st) cudaMemsetAsync(&flush_st->u_pending, 0, sizeof(int), s);
+}
+void launch_finalise_flush(const Fields& f, const Layout& L, LoopState* st, cudaStream_t s) {
+  { ++launch_counter(); k_finalise_flush<<<row_grid(L, false), TB, 0, s>>>(f, L, st); }
+  cudaMemsetAsync(&st->u_pending, 0, sizeof(int), s);
 }
 void launch_cg_init(const Fields& f, const Layout& L, const Geometry& g, const Reduce& rd, int mode, cudaStream_t s) {
   if (g.precond != 1) launch_precond(f, L, g, f.r, f.z, s);

@@ -52,6 +52,15 @@ void launch_finalise(const Fields& f, const Layout& L, cudaStream_t s);
 void launch_precond(const Fields& f, const Layout& L, const Geometry& g, const double* src, double* dst,
                     cudaStream_t s);
 void launch_cg_init(const Fields& f, const Layout& L, const Geometry& g, const Reduce& rd, int mode, cudaStream_t s);
+// residual + its norm + cg_init in one sweep (precond none or jac_diag): r, p (z), old_error,
+// initial_residual, rro
+void launch_residual_cg_init(const Fields& f, const Layout& L, const Geometry& g, const Reduce& rd, cudaStream_t s);
+// finalise with the pending deferred u update of the CG loop applied first
+void launch_finalise_flush(const Fields& f, const Layout& L, LoopState* st, cudaStream_t s);
+// finalise fused with field_summary (sums in st->red[0..4)); flush_st non-null: apply the
+// pending deferred u update first
+void launch_finalise_summary(const Fields& f, const Layout& L, double cell_vol, const Reduce& rd, LoopState* flush_st,
+                             cudaStream_t s);
 void launch_cg_calc_w(const Fields& f, const Layout& L, const Reduce& rd, cudaStream_t s);
 void launch_cg_calc_ur(const Fields& f, const Layout& L, const Geometry& g, double alpha, const Reduce& rd,
                        cudaStream_t s);

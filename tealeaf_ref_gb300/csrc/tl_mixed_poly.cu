@@ -173,6 +173,8 @@ struct PolyArgs {
   int first;           // level 0 synthesised: PPCG init_sd from r64, Chebyshev start from m.r
   int rows, nstrips, ntasks;
   int tx, t1, t2;      // TMA: indices in PolyMaps of the maps of x_in, c1_in, c2_in
+  int hold_row;        // test of the bounded wait: task 0 arms this row's mbarrier without issuing
+                       // its copies, so the wait for it runs out (-1: off)
   float ca[TB_S], cb[TB_S];
 };
 
@@ -286,6 +288,9 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
   const int lane = threadIdx.x & 31;
   const int task = blockIdx.x * TB_WARPS + (threadIdx.x >> 5);
   if (task >= a.ntasks) return;  // whole warps only
+  // an earlier sweep of this solve gave up on a staged row: its results are void, and so would
+  // this sweep's be; the solve reports TL_ERR_TIMEOUT
+  if (*reinterpret_cast<volatile const unsigned*>(a.m.err) != 0u) return;
   const Layout L = a.L;
   const MixFields& m = a.m;
   const int x0 = 1 + (task % a.nstrips) * TB_W;
@@ -330,6 +335,7 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the lanes' reads of these slots come first
     mbar_expect_tx(bar, bytes);
+    if (row == a.hold_row && task == 0) return;  // the test's row: armed, never copied
     if (row <= crow_max) {
       tma_row(coef(cs, 2), &pm.t[PM_CY], tmx, row, bar);
       if (row <= L.ny) {
@@ -563,6 +569,13 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
   }
 }
 
+// TL_POLY_TEST_HOLD=1: every blocked sweep launched makes warp 0 wait for a row whose copy is
+// never issued (the test of the bounded wait and of TL_ERR_TIMEOUT; TMA staging only).
+bool poly_test_hold() {
+  const char* e = getenv("TL_POLY_TEST_HOLD");
+  return e && e[0] == '1';
+}
+
 // Steps per blocked sweep: TB_S, or TL_POLY_STEPS_PER_SWEEP (1 .. TB_S) from the environment;
 // 1 selects the one-step kernels above (same results, bit for bit).
 int poly_steps_per_sweep() {
@@ -669,6 +682,7 @@ void launch_tb(PolyArgs a, int steps, bool tma, const PolyMaps& pm, cudaStream_t
   a.tx = map_index(a.m, a.x_in);
   a.t1 = map_index(a.m, a.c1_in);
   a.t2 = map_index(a.m, a.c2_in);
+  a.hold_row = poly_test_hold() ? 1 + TB_P : -1;  // task 0 starts its march at row 1
   ++launch_counter();
   if (tma) {
     switch (steps) {

@@ -71,6 +71,8 @@ SIGNATURES = {
     "tl_last_error": (C.c_char_p, []),
     "tl_set_device": (_I, [_I]),
     "tl_host_register": (_I, [_P, C.c_ulonglong]),
+    "tl_host_alloc": (_I, [C.c_ulonglong, C.POINTER(C.c_void_p)]),
+    "tl_host_free": (_I, [_P]),
     "tl_host_unregister": (_I, [_P]),
     "tl_create": (_I, [_I, _I, _I, _I, _I, _I, _D, _D, C.POINTER(_P)]),
     "tl_destroy": (_I, [_P]),
@@ -84,6 +86,7 @@ SIGNATURES = {
     "tl_calc_residual": (_I, [_P]),
     "tl_calc_2norm": (_I, [_P, _I, _DP]),
     "tl_finalise": (_I, [_P]),
+    "tl_finalise_field_summary": (_I, [_P, _DP, _DP, _DP, _DP]),
     "tl_cg_init": (_I, [_P, _DP]),
     "tl_cg_calc_w": (_I, [_P, _DP]),
     "tl_cg_calc_ur": (_I, [_P, _D, _DP]),
@@ -100,6 +103,7 @@ SIGNATURES = {
     "tl_jacobi_solve": (_I, [_P, _DP]),
     "tl_update_halo": (_I, [_P, _I, _I]),
     "tl_tea_leaf": (_I, [_P, C.POINTER(SolveOpts), _D, C.POINTER(SolveInfo)]),
+    "tl_tea_leaf_summary": (_I, [_P, C.POINTER(SolveOpts), _D, C.POINTER(SolveInfo), _DP]),
     "tl_reset_eigen": (_I, [_P]),
     "tl_cg_eigenvalues": (_I, [_DP, _DP, _I, _DP, _DP]),
     "tl_cheby_coefficients": (_I, [_D, _D, _I, _DP, _DP, _DP]),
@@ -143,17 +147,48 @@ def load(build_if_missing: bool = True):
         return L
 
 
-class PinnedArray:
-    """A numpy array whose pages are registered with the driver (tl_host_register)."""
+class _HostAllocation:
+    """Owner of one tl_host_alloc block: freed when the last numpy view of it is gone."""
 
-    def __init__(self, shape, dtype=np.float64):
-        self.array = np.zeros(shape, dtype=dtype)
-        _check(load().tl_host_register(self.array.ctypes.data, self.array.nbytes))
+    def __init__(self, nbytes: int):
+        p = C.c_void_p()
+        _check(load().tl_host_alloc(nbytes, C.byref(p)))
+        self.ptr = p.value
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                load().tl_host_free(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+
+class PinnedArray:
+    """A numpy array in page-locked host memory allocated by the CUDA driver (tl_host_alloc),
+    zero-filled; the memory lives as long as any view of ``array``.  ``register=True``
+    instead registers an ordinary numpy array (tl_host_register), the form a driver that owns
+    its arrays uses."""
+
+    def __init__(self, shape, dtype=np.float64, register: bool = False):
+        self._registered = register
+        if register:
+            self.array = np.zeros(shape, dtype=dtype)
+            _check(load().tl_host_register(self.array.ctypes.data, self.array.nbytes))
+            return
+        nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        owner = _HostAllocation(nbytes)
+        buf = (C.c_char * nbytes).from_address(owner.ptr)
+        buf._owner = owner  # the buffer (the base of every view) keeps the allocation alive
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+        self.array[...] = 0
 
     def close(self):
-        if self.array is not None:
+        if self.array is None:
+            return
+        if self._registered:
             load().tl_host_unregister(self.array.ctypes.data)
-            self.array = None
+        self.array = None
 
     def __del__(self):
         try:
@@ -317,6 +352,19 @@ class Chunk:
         _check(self.L.tl_tea_leaf(self.ptr, C.byref(o), dt, C.byref(info)))
         return info
 
+    def tea_leaf_summary(self, deck_or_opts, dt: Optional[float] = None):
+        """tea_leaf() of a time step followed by field_summary, the summary formed by the solve's
+        finalise sweep (tl_tea_leaf_summary): (SolveInfo, [vol, mass, ie, temp])."""
+        if isinstance(deck_or_opts, Deck):
+            o = opts_from_deck(deck_or_opts)
+            dt = deck_or_opts.initial_timestep if dt is None else dt
+        else:
+            o = deck_or_opts
+        info = SolveInfo()
+        out = np.zeros(4)
+        _check(self.L.tl_tea_leaf_summary(self.ptr, C.byref(o), dt, C.byref(info), _dp(out)))
+        return info, out
+
     # ---- adjoint (tl_adjoint_*) ----
     def adjoint_begin(self, max_steps: int, store_solutions: bool = True) -> None:
         _check(self.L.tl_adjoint_begin(self.ptr, max_steps, int(store_solutions)))
@@ -382,6 +430,12 @@ class Chunk:
 
     def finalise(self) -> None:
         _check(self.L.tl_finalise(self.ptr))
+
+    def finalise_field_summary(self) -> np.ndarray:
+        """tea_leaf_kernel_finalise then field_summary_kernel in one sweep."""
+        v = [C.c_double() for _ in range(4)]
+        _check(self.L.tl_finalise_field_summary(self.ptr, *[C.byref(x) for x in v]))
+        return np.array([x.value for x in v])
 
     def cg_init(self) -> float:
         return self._scalar(self.L.tl_cg_init)
@@ -463,15 +517,21 @@ def run_deck(deck: Deck, max_steps: Optional[int] = None, precision: str = "fp64
         while True:
             step += 1
             dt = deck.initial_timestep
-            solves.append(c.tea_leaf(opts, dt).as_dict())
+            # the summary steps of diffuse.f90:58-61 and the last step: the solve's finalise
+            # sweep forms the field summary too (tl_tea_leaf_summary)
+            done = (time + dt) + g_small > deck.end_time or step >= deck.end_step or \
+                bool(max_steps and step >= max_steps)
+            want = done or bool(deck.summary_frequency and step % deck.summary_frequency == 0)
+            if want:
+                info, summ = c.tea_leaf_summary(opts, dt)
+                summaries.append((step, summ))
+            else:
+                info = c.tea_leaf(opts, dt)
+            solves.append(info.as_dict())
             time = time + dt
-            done = time + g_small > deck.end_time or step >= deck.end_step or bool(max_steps and step >= max_steps)
-            if deck.summary_frequency and step % deck.summary_frequency == 0 and not done:
-                summaries.append((step, c.field_summary()))
             if vis and step % deck.visit_frequency == 0:
                 visit(step)
             if done:
-                summaries.append((step, c.field_summary()))
                 if vis:
                     visit(step)
                 break

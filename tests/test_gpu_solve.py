@@ -313,3 +313,66 @@ def test_setup_cache_follows_density_and_dt():
         c.tea_leaf(d, dt2)
         np.testing.assert_array_equal(c.download("u"), fresh(dens2, ener, dt2))
         c.wait_transfers()
+
+
+@pytest.mark.parametrize("case", [dict(), dict(nx=1030, ny=700), dict(reflective=True, nx=1030, ny=700),
+                                  dict(solver="ppcg", ppcg_inner_steps=10, ch_cg_presteps=20),
+                                  dict(solver="jacobi", max_iters=200, eps=1e-10),
+                                  dict(precision="mixed", nx=1030, ny=700)],
+                         ids=["cg-persistent", "cg-batched", "cg-reflective", "ppcg", "jacobi", "mixed-cg"])
+def test_tea_leaf_summary_bitwise(case):
+    """tl_tea_leaf_summary (finalise fused with field_summary, and with the CG loop's last
+    deferred u update on the batched path) gives the bits of tl_tea_leaf followed by
+    tl_field_summary: the summary, energy1, u and the iteration counts."""
+    from tealeaf_ref_gb300 import native
+
+    case = dict(case)
+    precision = case.pop("precision", "fp64")
+    kw = dict(nx=203, ny=151, steps=2, n_rect=4, n_circ=2, max_iters=20000)
+    kw.update(case)
+    d = small_deck(**kw)
+    opts = native.opts_from_deck(d, precision=precision)
+    runs = []
+    for fused in (False, True):
+        with native.Chunk.from_deck(d) as c:
+            out = []
+            for _ in range(d.end_step):
+                if fused:
+                    info, s = c.tea_leaf_summary(opts, d.initial_timestep)
+                else:
+                    info = c.tea_leaf(opts, d.initial_timestep)
+                    s = c.field_summary()
+                out.append((info.reported_iterations, s))
+            runs.append((out, c.download("energy1"), c.download("u")))
+    (o0, e0, u0), (o1, e1, u1) = runs
+    for (i0, s0), (i1, s1) in zip(o0, o1):
+        assert i0 == i1
+        np.testing.assert_array_equal(s0, s1)
+    np.testing.assert_array_equal(e0, e1)
+    np.testing.assert_array_equal(u0, u1)
+
+
+def test_finalise_field_summary_entry_point():
+    """tl_finalise_field_summary: the drop-in for tea_leaf_kernel_finalise followed by
+    field_summary_kernel gives the bits of the two calls, and the oracle's summary to 1e-12."""
+    from oracle import oracle
+    from tealeaf_ref_gb300 import native
+
+    d = small_deck(nx=97, ny=61, steps=1)
+    o = oracle.Chunk.from_deck(d)
+    o.common_init(d.initial_timestep)
+    o.finalise()
+    want = o.field_summary()
+    res = []
+    for fused in (False, True):
+        with native.Chunk.from_deck(d) as c:
+            c.common_init(d.initial_timestep)
+            if fused:
+                s = c.finalise_field_summary()
+            else:
+                c.finalise()
+                s = c.field_summary()
+            res.append((s, c.download("energy1")))
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    np.testing.assert_array_equal(res[0][1], res[1][1])
+    assert np.max(np.abs(res[1][0] - want) / np.abs(want)) < 1e-12

@@ -76,7 +76,8 @@ def test_oracle_reflective_and_jacobi_quirk():
 
 def test_exact_summary_helper_matches_serial_summary():
     """The correctly rounded field summary the full-size parity tests use agrees with the
-    oracle's serial field_summary where the serial sums' rounding is negligible (small meshes)."""
+    oracle's serial field_summary to within the serial sums' own rounding bound (4e-16 per
+    summed cell, as for the other reductions)."""
     import sys
     import os
     sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
@@ -85,4 +86,4 @@ def test_exact_summary_helper_matches_serial_summary():
     d = small_deck(nx=120, ny=77, steps=1)
     o = oracle.Chunk.from_deck(d)
     o.tea_leaf(d)
-    np.testing.assert_allclose(exact_summary(o), o.field_summary(), rtol=1e-13)
+    np.testing.assert_allclose(exact_summary(o), o.field_summary(), rtol=max(1e-12, 4e-16 * d.x_cells * d.y_cells))

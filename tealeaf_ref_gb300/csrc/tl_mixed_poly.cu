@@ -135,26 +135,33 @@ __global__ void k_poly_clear(MixFields m, Layout L) {
 }
 
 // ---- temporal blocking: up to TB_S polynomial steps per sweep ----------------------------
-// Each warp owns a strip of 128 columns (four per lane, 16-byte loads) with a TB_HX-column
-// halo on each side, TB_W output columns, and marches up a range of rows.  At march position
-// m, level 0 loads row m and level t = 1..S computes step t at row m - t from level t-1's rows
-// m-t-1 .. m-t+1 (a three-row register window per level) and level t-1's cell values of row m-t
-// (its output one march position earlier).  Horizontal neighbours come from the adjacent
-// lanes by shuffles.  Level 0's rows (coefficients and input state) are staged TB_P rows ahead
-// into per-warp shared-memory rings by asynchronous copies (cp.async), so a march step does not
-// wait for a load; every level reads the coefficients from the ring.  Warps never wait for one
-// another.  Level t is exact on local columns
-// [t, 128-t): with S <= TB_HX the output columns are exact.  Every cell runs the one-step
-// kernels' arithmetic in the same order, so S steps here give the bits of S one-step sweeps.
-// Traffic per S steps: the state and the coefficients read once (x 128/TB_W for the halo),
-// the state written once.
-constexpr int TB_S = 4;                // steps per sweep at most
-constexpr int TB_HX = 4;               // halo columns on each side of a warp strip
-constexpr int TB_W = 128 - 2 * TB_HX;  // output columns per warp strip
-constexpr int TB_WARPS = 4;            // warps per CTA
-constexpr int TB_P = 2;                // rows staged ahead by asynchronous copies
-constexpr int TB_PF = 8;               // L2 prefetch distance in rows
+// Each warp owns a strip of 32*CPL columns (CPL columns per lane: 2, with 8-byte accesses, or
+// 4, with 16-byte accesses) with a TB_HX-column halo on each side, 32*CPL - 2*TB_HX output
+// columns, and marches up a range of rows.  At march position m, level 0 loads row m and level
+// t = 1..S computes step t at row m - t from level t-1's rows m-t-1 .. m-t+1 (a three-row
+// register window per level) and level t-1's cell values of row m-t (its output one march
+// position earlier).  Horizontal neighbours come from the adjacent lanes by shuffles.  Level
+// 0's rows (coefficients and input state) are staged TB_P rows ahead into per-warp
+// shared-memory rings by TMA tensor copies (or cp.async), so a march step does not wait for a
+// load; every level reads the coefficients from the ring.  Warps never wait for one another.
+// Level t is exact on local columns [t, 32*CPL-t): with S <= TB_HX the output columns are
+// exact.  Every cell runs the one-step kernels' arithmetic in the same order, so S steps here
+// give the bits of S one-step sweeps, whatever CPL.  Traffic per S steps: the state and the
+// coefficients read once (x 32*CPL / output width, for the halo), the state written once.
+// CPL 2 halves the register windows and the shared memory of a warp (more resident warps)
+// for twice the halo overhead of CPL 4; CPL 4 is the faster (see POLY_CPL).
+constexpr int TB_S = 4;      // steps per sweep at most
+constexpr int TB_HX = 4;     // halo columns on each side of a warp strip
+constexpr int TB_WARPS = 4;  // warps per CTA
+constexpr int TB_P = 2;      // rows staged ahead by asynchronous copies
+constexpr int TB_PF = 8;     // L2 prefetch distance in rows
 constexpr unsigned FULL = 0xffffffffu;
+
+template <int CPL>
+struct TbGeom {
+  static constexpr int SWX = 32 * CPL;        // strip width, halo included (the TMA box width)
+  static constexpr int W = SWX - 2 * TB_HX;   // output columns per strip
+};
 
 enum { POLY_PPCG = 0, POLY_CHEBY = 1 };
 
@@ -179,7 +186,7 @@ struct PolyArgs {
 };
 
 // Tensor maps (TMA descriptors) of the fields a blocked sweep reads: each a 2-D view
-// (ld x (ny+2)) with a 128-element by 1-row box.
+// (ld x (ny+2)) with a (32*CPL)-element by 1-row box.
 enum { PM_P = 0, PM_P2, PM_R, PM_W, PM_D, PM_E, PM_CX, PM_CY, PM_DI, PM_R64, PM_N };
 struct PolyMaps {
   CUtensorMap t[PM_N];
@@ -187,29 +194,34 @@ struct PolyMaps {
 
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
-// columns j+i with lo <= j+i <= hi
-__device__ __forceinline__ void store4(float* __restrict__ p, long long c, const float (&v)[4], int lo, int hi,
-                                       int j) {
-  if (j >= lo && j + 3 <= hi) {
-    *reinterpret_cast<float4*>(p + c) = make_float4(v[0], v[1], v[2], v[3]);
+// columns j+i with lo <= j+i <= hi: one vector store when all CPL lie there
+template <int CPL>
+__device__ __forceinline__ void store_cols(float* __restrict__ p, long long c, const float (&v)[CPL], int lo, int hi,
+                                           int j) {
+  if (j >= lo && j + CPL - 1 <= hi) {
+    if constexpr (CPL == 4)
+      *reinterpret_cast<float4*>(p + c) = make_float4(v[0], v[1], v[2], v[3]);
+    else
+      *reinterpret_cast<float2*>(p + c) = make_float2(v[0], v[1]);
   } else {
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < CPL; ++i)
       if (j + i >= lo && j + i <= hi) p[c + i] = v[i];
   }
 }
 
 // Per-warp shared memory of the blocked sweep: a ring of RING coefficient rows (di, cx, cy, and
-// Chebyshev's right-hand side; 132 floats per array row) and a ring of TB_P+1 input-state rows.
-// With TMA the array rows are 128 floats apart (every TMA destination 128-byte aligned; the
-// lane that reads column j+4 past its warp's strip is a halo lane) and TB_P+1 mbarriers follow.
-template <int MODE, int S, bool TMA>
+// Chebyshev's right-hand side; CP floats per array row) and a ring of TB_P+1 input-state rows.
+// With TMA the array rows are 32*CPL floats apart (every TMA destination 128-byte aligned; the
+// lane that reads column j+CPL past its warp's strip is a halo lane) and TB_P+1 mbarriers follow.
+template <int MODE, int S, bool TMA, int CPL>
 struct TbSmem {
+  static constexpr int SWX = TbGeom<CPL>::SWX;
   static constexpr int NC = MODE == POLY_PPCG ? 3 : 4;
   static constexpr int RING = S + 1 + TB_P;
-  static constexpr int CP = TMA ? 128 : 132;                          // floats per coefficient array row
-  static constexpr int SSLOT = (MODE == POLY_PPCG ? 3 : 2) * 128;  // floats (PPCG: or 128 doubles)
-  static constexpr int BAR = TMA ? 32 : 0;                          // floats: the mbarriers (128 B)
+  static constexpr int CP = TMA ? SWX : SWX + 4;                 // floats per coefficient array row
+  static constexpr int SSLOT = (MODE == POLY_PPCG ? 3 : 2) * SWX;  // floats (PPCG: or SWX doubles)
+  static constexpr int BAR = TMA ? 32 : 0;                        // floats: the mbarriers (128 B)
   static constexpr int WARP_FLOATS = RING * NC * CP + (TB_P + 1) * SSLOT + BAR;
   static constexpr int BYTES = TB_WARPS * WARP_FLOATS * 4;
 };
@@ -243,7 +255,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
   }
   return false;
 }
-// one 128-element row box of a 2-D tensor map into shared memory, completing on bar
+// one row box of a 2-D tensor map into shared memory, completing on bar
 __device__ __forceinline__ void tma_row(void* dst, const CUtensorMap* map, int x, int y, unsigned long long* bar) {
   asm volatile(
       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
@@ -252,39 +264,45 @@ __device__ __forceinline__ void tma_row(void* dst, const CUtensorMap* map, int x
       : "memory");
 }
 
-__device__ __forceinline__ void cp_async16(float* dst, const void* src) {
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* dst, const void* src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src));
+  if constexpr (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src));
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src));
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N)); }
 
-// columns j .. j+3 of a float row into shared memory: an asynchronous 16-byte copy when all four
-// lie in [lo, hi], else guarded loads (zero outside)
-__device__ __forceinline__ void stage4(float* dst, const float* __restrict__ src, int j, int lo, int hi) {
-  if (j >= lo && j + 3 <= hi) {
-    cp_async16(dst, src);
+// columns j .. j+CPL-1 of a float row into shared memory: one asynchronous copy when all lie in
+// [lo, hi], else guarded loads (zero outside)
+template <int CPL>
+__device__ __forceinline__ void stage_cols(float* dst, const float* __restrict__ src, int j, int lo, int hi) {
+  if (j >= lo && j + CPL - 1 <= hi) {
+    cp_async<4 * CPL>(dst, src);
   } else {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) dst[i] = (j + i >= lo && j + i <= hi) ? __ldg(src + i) : 0.f;
+    for (int i = 0; i < CPL; ++i) dst[i] = (j + i >= lo && j + i <= hi) ? __ldg(src + i) : 0.f;
   }
 }
-__device__ __forceinline__ void stage4d(double* dst, const double* __restrict__ src, int j, int lo, int hi) {
-  if (j >= lo && j + 3 <= hi) {
-    cp_async16(reinterpret_cast<float*>(dst), src);
-    cp_async16(reinterpret_cast<float*>(dst + 2), src + 2);
+template <int CPL>
+__device__ __forceinline__ void stage_cols_d(double* dst, const double* __restrict__ src, int j, int lo, int hi) {
+  if (j >= lo && j + CPL - 1 <= hi) {
+#pragma unroll
+    for (int i = 0; i < CPL; i += 2) cp_async<16>(dst + i, src + i);
   } else {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) dst[i] = (j + i >= lo && j + i <= hi) ? __ldg(src + i) : 0.0;
+    for (int i = 0; i < CPL; ++i) dst[i] = (j + i >= lo && j + i <= hi) ? __ldg(src + i) : 0.0;
   }
 }
 
-template <int MODE, int S, bool TMA>
+template <int MODE, int S, bool TMA, int CPL>
 __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __grid_constant__ PolyMaps pm) {
   constexpr bool PPCG = MODE == POLY_PPCG;
-  using SM = TbSmem<MODE, S, TMA>;
-  constexpr int NC = SM::NC, RING = SM::RING, CP = SM::CP;
+  using SM = TbSmem<MODE, S, TMA, CPL>;
+  constexpr int NC = SM::NC, RING = SM::RING, CP = SM::CP, SWX = SM::SWX, W = TbGeom<CPL>::W;
   const int lane = threadIdx.x & 31;
   const int task = blockIdx.x * TB_WARPS + (threadIdx.x >> 5);
   if (task >= a.ntasks) return;  // whole warps only
@@ -293,18 +311,18 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
   if (*reinterpret_cast<volatile const unsigned*>(a.m.err) != 0u) return;
   const Layout L = a.L;
   const MixFields& m = a.m;
-  const int x0 = 1 + (task % a.nstrips) * TB_W;
+  const int x0 = 1 + (task % a.nstrips) * W;
   const int k0 = 1 + (task / a.nstrips) * a.rows;
   const int k1 = min(k0 + a.rows - 1, L.ny);
-  const int j = x0 - TB_HX + 4 * lane;  // this lane's first column
-  const int out0 = x0, out1 = min(x0 + TB_W - 1, L.nx);
-  const int lc = 4 * lane;
+  const int j = x0 - TB_HX + CPL * lane;  // this lane's first column
+  const int out0 = x0, out1 = min(x0 + W - 1, L.nx);
+  const int lc = CPL * lane;
   extern __shared__ __align__(128) float tb_smem[];
   float* const wbase = tb_smem + (threadIdx.x >> 5) * SM::WARP_FLOATS;
   // ring slots: row r sits in coefficient slot (r - mstart) mod RING and state slot
   // (r - mstart) mod (TB_P+1); the march keeps the slots of row mm in running counters
   auto coef = [&](int slot, int arr) { return wbase + (slot * NC + arr) * CP; };
-  auto state = [&](int slot, int arr) { return wbase + RING * NC * CP + slot * SM::SSLOT + arr * 128; };
+  auto state = [&](int slot, int arr) { return wbase + RING * NC * CP + slot * SM::SSLOT + arr * SWX; };
   constexpr int SR = TB_P + 1;
   unsigned long long* const bars =
       reinterpret_cast<unsigned long long*>(wbase + RING * NC * CP + SR * SM::SSLOT);  // TMA: one per state slot
@@ -325,9 +343,10 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
   // (columns past the field's rows read as zero); an empty row only arrives
   auto issue_row_tma = [&](int row, int cs, int ss) {
     if (lane != 0) return;
+    constexpr unsigned RB = 4u * SWX;  // bytes of one float row box
     unsigned bytes = 0;
-    if (row <= crow_max) bytes += (row <= L.ny ? (PPCG ? 3 : 4) : 1) * 512;
-    if (row <= srow_max) bytes += a.first ? (PPCG ? 1024 : 0) : (PPCG ? 3 : 2) * 512;
+    if (row <= crow_max) bytes += (row <= L.ny ? (PPCG ? 3 : 4) : 1) * RB;
+    if (row <= srow_max) bytes += a.first ? (PPCG ? 2 * RB : 0) : (PPCG ? 3 : 2) * RB;
     unsigned long long* bar = &bars[ss];
     if (bytes == 0) {
       mbar_arrive(bar);
@@ -364,32 +383,32 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
     }
     if (row <= crow_max) {
       const long long c = L.at(j, row);
-      stage4(coef(cs, 2) + lc, m.cy + c, j, 1, L.nx);
+      stage_cols<CPL>(coef(cs, 2) + lc, m.cy + c, j, 1, L.nx);
       if (row <= L.ny) {
-        stage4(coef(cs, 0) + lc, m.di + c, j, 1, L.nx);
-        stage4(coef(cs, 1) + lc, m.cx + c, j, 1, L.nx + 1);
-        if (!PPCG) stage4(coef(cs, 3) + lc, m.r + c, j, 1, L.nx);
+        stage_cols<CPL>(coef(cs, 0) + lc, m.di + c, j, 1, L.nx);
+        stage_cols<CPL>(coef(cs, 1) + lc, m.cx + c, j, 1, L.nx + 1);
+        if (!PPCG) stage_cols<CPL>(coef(cs, 3) + lc, m.r + c, j, 1, L.nx);
       }
     }
     if (row <= srow_max) {
       const long long c = L.at(j, row);
       if (a.first) {
-        if (PPCG) stage4d(reinterpret_cast<double*>(state(ss, 0)) + lc, a.r64 + c, j, 1, L.nx);
+        if (PPCG) stage_cols_d<CPL>(reinterpret_cast<double*>(state(ss, 0)) + lc, a.r64 + c, j, 1, L.nx);
       } else {
-        stage4(state(ss, 0) + lc, a.x_in + c, j, 1, L.nx);
-        stage4(state(ss, 1) + lc, a.c1_in + c, j, 1, L.nx);
-        if (PPCG) stage4(state(ss, 2) + lc, a.c2_in + c, j, 1, L.nx);
+        stage_cols<CPL>(state(ss, 0) + lc, a.x_in + c, j, 1, L.nx);
+        stage_cols<CPL>(state(ss, 1) + lc, a.c1_in + c, j, 1, L.nx);
+        if (PPCG) stage_cols<CPL>(state(ss, 2) + lc, a.c2_in + c, j, 1, L.nx);
       }
     }
     cp_async_commit();
   };
-  float X[S][3][4];   // level t < S: stencil variable of rows (newest-2, newest-1, newest)
-  float C1[S][2][4];  // level t < S: rtemp | p of rows (newest-1, newest)
-  float C2[S][2][4];  // level t < S: utemp of rows (newest-1, newest)
+  float X[S][3][CPL];   // level t < S: stencil variable of rows (newest-2, newest-1, newest)
+  float C1[S][2][CPL];  // level t < S: rtemp | p of rows (newest-1, newest)
+  float C2[S][2][CPL];  // level t < S: utemp of rows (newest-1, newest)
 #pragma unroll
   for (int t = 0; t < S; ++t)
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < CPL; ++i) {
       X[t][0][i] = X[t][1][i] = X[t][2][i] = 0.f;
       C1[t][0][i] = C1[t][1][i] = C2[t][0][i] = C2[t][1][i] = 0.f;
     }
@@ -405,8 +424,8 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
       if (ss >= SR) ss -= SR;
       issue_row(mm + TB_P, cs, ss);
     }
-    const int pf = mm + TB_PF;  // L2 prefetch further ahead
-    if (pf <= srow_max && j >= 1 && j + 3 <= L.nx) {
+    const int pf = mm + TB_PF;  // L2 prefetch further ahead, one lane per 32-float stretch
+    if (pf <= srow_max && (lc & 31) == 0 && j >= 1 && j + CPL - 1 <= L.nx) {
       const long long c = L.at(j, pf);
       if (!a.first) {
         prefetch_l2(a.x_in + c);
@@ -437,13 +456,15 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
     }
     __syncwarp();
     // ---- level 0: the sweep's input at row mm ----
-    float nx[4] = {0.f, 0.f, 0.f, 0.f}, n1[4] = {0.f, 0.f, 0.f, 0.f}, n2[4] = {0.f, 0.f, 0.f, 0.f};
+    float nx[CPL], n1[CPL], n2[CPL];
+#pragma unroll
+    for (int i = 0; i < CPL; ++i) nx[i] = n1[i] = n2[i] = 0.f;
     if (mm <= srow_max) {
       if (a.first) {
         if (PPCG) {
           const double* rs = reinterpret_cast<const double*>(state(sslot, 0)) + lc;
 #pragma unroll
-          for (int i = 0; i < 4; ++i) {
+          for (int i = 0; i < CPL; ++i) {
             const float rv = (float)rs[i];
             n1[i] = rv;
             nx[i] = rv * a.inv_theta;
@@ -452,14 +473,14 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
         } else {
           const float* rs = coef(cslot, 3) + lc;
 #pragma unroll
-          for (int i = 0; i < 4; ++i) {
+          for (int i = 0; i < CPL; ++i) {
             nx[i] = rs[i] * a.inv_theta;
             n1[i] = nx[i];
           }
         }
       } else {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < CPL; ++i) {
           nx[i] = state(sslot, 0)[lc + i];
           n1[i] = state(sslot, 1)[lc + i];
           if (PPCG) n2[i] = state(sslot, 2)[lc + i];
@@ -467,7 +488,7 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
       }
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < CPL; ++i) {
       X[0][0][i] = X[0][1][i];
       X[0][1][i] = X[0][2][i];
       X[0][2][i] = nx[i];
@@ -481,7 +502,9 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
     for (int t = 1; t <= S; ++t) {
       const int q = mm - t;
       const bool act = q >= max(1, k0 - (S - t)) && q <= min(L.ny, k1 + (S - t));  // uniform per warp
-      float ox[4] = {0.f, 0.f, 0.f, 0.f}, o1[4] = {0.f, 0.f, 0.f, 0.f}, o2[4] = {0.f, 0.f, 0.f, 0.f};
+      float ox[CPL], o1[CPL], o2[CPL];
+#pragma unroll
+      for (int i = 0; i < CPL; ++i) ox[i] = o1[i] = o2[i] = 0.f;
       if (act) {
         int qs = cslot - t, qs1 = cslot - t + 1;  // slots of rows q and q+1
         if (qs < 0) qs += RING;
@@ -490,29 +513,29 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
         const float* rcx = coef(qs, 1) + lc;
         const float* rcy = coef(qs, 2) + lc;
         const float* rcy1 = coef(qs1, 2) + lc;
-        float di[4], cxv[4], cyb[4], cyt[4], rhs[4];
+        float di[CPL], cxv[CPL], cyb[CPL], cyt[CPL], rhs[CPL];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < CPL; ++i) {
           di[i] = rdi[i];
           cxv[i] = rcx[i];
           cyb[i] = rcy[i];
           cyt[i] = rcy1[i];
           rhs[i] = PPCG ? 0.f : coef(qs, NC - 1)[lc + i];
         }
-        const float cx4 = rcx[4];                                       // cx at column j+4
-        const float left = __shfl_up_sync(FULL, X[t - 1][1][3], 1);     // column j-1
-        const float right = __shfl_down_sync(FULL, X[t - 1][1][0], 1);  // column j+4
+        const float cxn = rcx[CPL];                                          // cx at column j+CPL
+        const float left = __shfl_up_sync(FULL, X[t - 1][1][CPL - 1], 1);  // column j-1
+        const float right = __shfl_down_sync(FULL, X[t - 1][1][0], 1);     // column j+CPL
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < CPL; ++i) {
           const float vc = X[t - 1][1][i];
           const float off = PPCG ? vc : 0.f;  // mirror (PPCG's sd) or zero (Chebyshev's d)
           float vl = (i == 0) ? left : X[t - 1][1][i - 1];
-          float vr = (i == 3) ? right : X[t - 1][1][i + 1];
+          float vr = (i == CPL - 1) ? right : X[t - 1][1][i + 1];
           if (j + i == 1) vl = off;
           if (j + i == L.nx) vr = off;
           const float vb = (q > 1) ? X[t - 1][0][i] : off;
           const float vt = (q < L.ny) ? X[t - 1][2][i] : off;
-          const float cr1 = (i == 3) ? cx4 : cxv[i + 1];
+          const float cr1 = (i == CPL - 1) ? cxn : cxv[i + 1];
           float av = di[i] * vc;
           av = fmaf(-cyt[i], vt, av);
           av = fmaf(-cyb[i], vb, av);
@@ -534,7 +557,7 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
       }
       if (t < S) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < CPL; ++i) {
           X[t][0][i] = X[t][1][i];
           X[t][1][i] = X[t][2][i];
           X[t][2][i] = ox[i];
@@ -547,12 +570,12 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
         const long long c = L.at(j, q);
         if (PPCG && a.z) {
 #pragma unroll
-          for (int i = 0; i < 4; ++i)
+          for (int i = 0; i < CPL; ++i)
             if (j + i >= out0 && j + i <= out1) a.z[c + i] = (double)o2[i];
         } else {
-          store4(a.x_out, c, ox, out0, out1, j);
-          store4(a.c1_out, c, o1, out0, out1, j);
-          if (PPCG) store4(a.c2_out, c, o2, out0, out1, j);
+          store_cols<CPL>(a.x_out, c, ox, out0, out1, j);
+          store_cols<CPL>(a.c1_out, c, o1, out0, out1, j);
+          if (PPCG) store_cols<CPL>(a.c2_out, c, o2, out0, out1, j);
         }
       }
     }
@@ -584,23 +607,54 @@ int poly_steps_per_sweep() {
   return v < 1 ? 1 : (v > TB_S ? TB_S : v);
 }
 
-void tb_tasks(PolyArgs& a, const Layout& L) {
-  a.nstrips = (L.nx + TB_W - 1) / TB_W;
-  // about two waves of 12 resident warps per SM, at least 32 rows per task (the warm-up of the
-  // levels costs ~S rows per task)
-  const long long target = 152LL * 12 * 2;
+// Columns per lane of the blocked sweeps: POLY_CPL, or TL_POLY_COLS (2 or 4) from the
+// environment (same results, bit for bit).  At 4096^2 the 2-column strips (79-96 registers,
+// 20-24 resident warps per SM instead of 12) measured slower: 53.1 against 49.1 us per FP32
+// PPCG step and 47.0 against 39.9 us per Chebyshev step -- the doubled halo costs more than
+// the occupancy gains.
+constexpr int POLY_CPL = 4;
+int poly_cols() {
+  const char* e = getenv("TL_POLY_COLS");
+  if (e && (e[0] == '2' || e[0] == '4')) return e[0] - '0';
+  return POLY_CPL;
+}
+
+// Warp tasks: strips x row ranges, about two waves of the resident warps (warps_per_sm),
+// at least 32 rows per task (the warm-up of the levels costs ~S rows per task).
+void tb_tasks(PolyArgs& a, const Layout& L, int cpl, int warps_per_sm) {
+  const int w = cpl == 4 ? TbGeom<4>::W : TbGeom<2>::W;
+  a.nstrips = (L.nx + w - 1) / w;
+  const long long target = 152LL * warps_per_sm * 2;
   int rows = (int)(((long long)L.ny * a.nstrips + target - 1) / target);
   rows = rows < 32 ? 32 : (rows > 256 ? 256 : rows);
   a.rows = rows;
   a.ntasks = a.nstrips * ((L.ny + rows - 1) / rows);
 }
 
-template <int MODE, int S, bool TMA>
+template <int MODE, int S, bool TMA, int CPL>
 void launch_tb_s(const PolyArgs& a, const PolyMaps& pm, dim3 grid, cudaStream_t s) {
-  constexpr int bytes = TbSmem<MODE, S, TMA>::BYTES;
+  constexpr int bytes = TbSmem<MODE, S, TMA, CPL>::BYTES;
   // above the 48 KB default: the attribute is set on the current device before each launch
-  cudaFuncSetAttribute(k_poly_tb<MODE, S, TMA>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  k_poly_tb<MODE, S, TMA><<<grid, 32 * TB_WARPS, bytes, s>>>(a, pm);
+  cudaFuncSetAttribute(k_poly_tb<MODE, S, TMA, CPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  k_poly_tb<MODE, S, TMA, CPL><<<grid, 32 * TB_WARPS, bytes, s>>>(a, pm);
+}
+
+// resident warps per SM of the S = TB_S instance (the one most sweeps use)
+template <int MODE, bool TMA, int CPL>
+int tb_resident_warps() {
+  static const int w = [] {
+    constexpr int bytes = TbSmem<MODE, TB_S, TMA, CPL>::BYTES;
+    cudaFuncSetAttribute(k_poly_tb<MODE, TB_S, TMA, CPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_poly_tb<MODE, TB_S, TMA, CPL>, 32 * TB_WARPS, bytes) !=
+            cudaSuccess ||
+        per_sm < 1) {
+      cudaGetLastError();
+      per_sm = 3;
+    }
+    return per_sm * TB_WARPS;
+  }();
+  return w;
 }
 
 // ---- tensor maps ----
@@ -625,12 +679,12 @@ PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
   return fn;
 }
 
-// a (ld x (ny+2)) view of one field with a 128 x 1 box; cached per (address, layout, type)
-bool tmap_of(const void* base, const Layout& L, bool f64, CUtensorMap* out) {
+// a (ld x (ny+2)) view of one field with a box_w x 1 box; cached per (address, layout, type, box)
+bool tmap_of(const void* base, const Layout& L, bool f64, int box_w, CUtensorMap* out) {
   static std::mutex mu;
-  static std::map<std::tuple<const void*, int, int, bool>, CUtensorMap> cache;
+  static std::map<std::tuple<const void*, int, int, bool, int>, CUtensorMap> cache;
   std::lock_guard<std::mutex> lock(mu);
-  const auto key = std::make_tuple(base, L.ld, L.ny, f64);
+  const auto key = std::make_tuple(base, L.ld, L.ny, f64, box_w);
   auto it = cache.find(key);
   if (it != cache.end()) {
     *out = it->second;
@@ -640,7 +694,7 @@ bool tmap_of(const void* base, const Layout& L, bool f64, CUtensorMap* out) {
   if (!enc) return false;
   const cuuint64_t dims[2] = {(cuuint64_t)L.ld, (cuuint64_t)L.ny + 2};
   const cuuint64_t strides[1] = {(cuuint64_t)L.ld * (f64 ? 8 : 4)};
-  const cuuint32_t box[2] = {128, 1};
+  const cuuint32_t box[2] = {(cuuint32_t)box_w, 1};
   const cuuint32_t estr[2] = {1, 1};
   CUtensorMap m;
   if (enc(&m, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims,
@@ -653,13 +707,13 @@ bool tmap_of(const void* base, const Layout& L, bool f64, CUtensorMap* out) {
 }
 
 // the maps of every field a blocked sweep may read; false if TMA is off or unavailable
-bool poly_maps(const MixFields& m, const Layout& L, const double* r64, PolyMaps* pm) {
+bool poly_maps(const MixFields& m, const Layout& L, const double* r64, int box_w, PolyMaps* pm) {
   if (!poly_use_tma()) return false;
   const float* f[PM_R64] = {m.p, m.p2, m.r, m.w, m.d, m.e, m.cx, m.cy, m.di};
   for (int i = 0; i < PM_R64; ++i)
-    if (!tmap_of(f[i], L, false, &pm->t[i])) return false;
+    if (!tmap_of(f[i], L, false, box_w, &pm->t[i])) return false;
   if (r64) {
-    if (!tmap_of(r64, L, true, &pm->t[PM_R64])) return false;
+    if (!tmap_of(r64, L, true, box_w, &pm->t[PM_R64])) return false;
   } else {
     pm->t[PM_R64] = pm->t[PM_R];  // not read
   }
@@ -676,29 +730,37 @@ int map_index(const MixFields& m, const float* p) {
   return PM_R;  // (the first sweep reads no state map)
 }
 
+template <int MODE, bool TMA, int CPL>
+void launch_tb_cpl(const PolyArgs& a, int steps, const PolyMaps& pm, dim3 grid, cudaStream_t s) {
+  switch (steps) {
+    case 1: launch_tb_s<MODE, 1, TMA, CPL>(a, pm, grid, s); break;
+    case 2: launch_tb_s<MODE, 2, TMA, CPL>(a, pm, grid, s); break;
+    case 3: launch_tb_s<MODE, 3, TMA, CPL>(a, pm, grid, s); break;
+    default: launch_tb_s<MODE, 4, TMA, CPL>(a, pm, grid, s); break;
+  }
+}
+
 template <int MODE>
-void launch_tb(PolyArgs a, int steps, bool tma, const PolyMaps& pm, cudaStream_t s) {
+void launch_tb(PolyArgs a, int steps, bool tma, int cpl, const PolyMaps& pm, cudaStream_t s) {
   const dim3 grid((a.ntasks + TB_WARPS - 1) / TB_WARPS);
   a.tx = map_index(a.m, a.x_in);
   a.t1 = map_index(a.m, a.c1_in);
   a.t2 = map_index(a.m, a.c2_in);
   a.hold_row = poly_test_hold() ? 1 + TB_P : -1;  // task 0 starts its march at row 1
   ++launch_counter();
-  if (tma) {
-    switch (steps) {
-      case 1: launch_tb_s<MODE, 1, true>(a, pm, grid, s); break;
-      case 2: launch_tb_s<MODE, 2, true>(a, pm, grid, s); break;
-      case 3: launch_tb_s<MODE, 3, true>(a, pm, grid, s); break;
-      default: launch_tb_s<MODE, 4, true>(a, pm, grid, s); break;
-    }
+  if (cpl == 4) {
+    if (tma) launch_tb_cpl<MODE, true, 4>(a, steps, pm, grid, s);
+    else launch_tb_cpl<MODE, false, 4>(a, steps, pm, grid, s);
   } else {
-    switch (steps) {
-      case 1: launch_tb_s<MODE, 1, false>(a, pm, grid, s); break;
-      case 2: launch_tb_s<MODE, 2, false>(a, pm, grid, s); break;
-      case 3: launch_tb_s<MODE, 3, false>(a, pm, grid, s); break;
-      default: launch_tb_s<MODE, 4, false>(a, pm, grid, s); break;
-    }
+    if (tma) launch_tb_cpl<MODE, true, 2>(a, steps, pm, grid, s);
+    else launch_tb_cpl<MODE, false, 2>(a, steps, pm, grid, s);
   }
+}
+
+template <int MODE>
+int tb_warps(bool tma, int cpl) {
+  if (cpl == 4) return tma ? tb_resident_warps<MODE, true, 4>() : tb_resident_warps<MODE, false, 4>();
+  return tma ? tb_resident_warps<MODE, true, 2>() : tb_resident_warps<MODE, false, 2>();
 }
 
 }  // namespace
@@ -713,9 +775,10 @@ void launch_poly_ppcg_inner(const Fields& f, const MixFields& m, const Layout& L
     a.L = L;
     a.r64 = f.r;
     a.inv_theta = (float)(1.0 / theta);
-    tb_tasks(a, L);
+    const int cpl = poly_cols();
     PolyMaps pm;
-    const bool tma = poly_maps(m, L, f.r, &pm);
+    const bool tma = poly_maps(m, L, f.r, 32 * cpl, &pm);
+    tb_tasks(a, L, cpl, tb_warps<POLY_PPCG>(tma, cpl));
     int done = 0, par = 0;
     while (done < inner_steps) {
       const int st = inner_steps - done < blk ? inner_steps - done : blk;
@@ -731,7 +794,7 @@ void launch_poly_ppcg_inner(const Fields& f, const MixFields& m, const Layout& L
         a.cb[i] = i < st ? (float)ch_b[done + 1 + i] : 0.f;
       }
       a.z = done + st == inner_steps ? f.z : nullptr;
-      launch_tb<POLY_PPCG>(a, st, tma, pm, s);
+      launch_tb<POLY_PPCG>(a, st, tma, cpl, pm, s);
       done += st;
       par ^= 1;
     }
@@ -763,9 +826,10 @@ void launch_poly_cheby(const MixFields& m, const Layout& L, double theta, int st
     a.m = m;
     a.L = L;
     a.inv_theta = (float)(1.0 / theta);
-    tb_tasks(a, L);
+    const int cpl = poly_cols();
     PolyMaps pm;
-    const bool tma = poly_maps(m, L, nullptr, &pm);
+    const bool tma = poly_maps(m, L, nullptr, 32 * cpl, &pm);
+    tb_tasks(a, L, cpl, tb_warps<POLY_CHEBY>(tma, cpl));
     const int nb = (iters + blk - 1) / blk;
     const float* din = nullptr;
     const float* pin = nullptr;
@@ -781,7 +845,7 @@ void launch_poly_cheby(const MixFields& m, const Layout& L, double theta, int st
         a.ca[i] = i < st ? (float)ch_a[b * blk + 1 + i] : 0.f;
         a.cb[i] = i < st ? (float)ch_b[b * blk + 1 + i] : 0.f;
       }
-      launch_tb<POLY_CHEBY>(a, st, tma, pm, s);
+      launch_tb<POLY_CHEBY>(a, st, tma, cpl, pm, s);
       din = a.x_out;
       pin = a.c1_out;
     }

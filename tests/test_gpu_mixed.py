@@ -151,17 +151,21 @@ def test_mixed_rejected_for_jacobi_and_preconditioners():
 @pytest.mark.parametrize("reflective", [False, True])
 def test_blocked_poly_sweeps_bitwise(solver, reflective, monkeypatch):
     """The temporally blocked FP32 sweeps (several polynomial steps per pass over the mesh)
-    give the bits of the one-step sweeps: same solution and iteration counts for 1, 3 and 4
-    steps per sweep, on a mesh whose width and height cut the warp strips and row ranges
-    raggedly."""
+    give the bits of the one-step sweeps: same solution and iteration counts for 3 and 4
+    steps per sweep, 2 or 4 columns per lane, TMA or cp.async staging, on a mesh whose width
+    and height cut the warp strips and row ranges raggedly."""
     from tealeaf_ref_gb300 import native
 
     d = small_deck(nx=301, ny=133, steps=2, n_rect=4, n_circ=2, solver=solver, ppcg_inner_steps=10,
                    ch_cg_presteps=20, reflective=reflective, max_iters=20000)
     opts = native.opts_from_deck(d, precision="mixed")
     runs = []
-    for per_sweep in ("1", "4", "3"):
+    # steps per sweep x columns per lane of the warp strips (2 or 4) x staging (TMA or cp.async)
+    for per_sweep, cols, tma in (("1", "2", "1"), ("4", "2", "1"), ("3", "2", "1"), ("4", "4", "1"),
+                                 ("3", "4", "1"), ("4", "2", "0"), ("4", "4", "0")):
         monkeypatch.setenv("TL_POLY_STEPS_PER_SWEEP", per_sweep)
+        monkeypatch.setenv("TL_POLY_COLS", cols)
+        monkeypatch.setenv("TL_POLY_TMA", tma)
         with native.Chunk.from_deck(d) as c:
             its = [c.tea_leaf(opts, d.initial_timestep).reported_iterations for _ in range(d.end_step)]
             runs.append((c.download("u"), its))

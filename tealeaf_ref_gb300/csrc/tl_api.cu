@@ -1182,13 +1182,15 @@ namespace {
 int ensure_mix(tl_ctx* c) {
   if (c->mix_slab) return TL_OK;
   const size_t fb = ((size_t)c->L.elems() * sizeof(float) + 4 * 256 + 255) / 256 * 256;
-  CK(cudaMalloc(&c->mix_slab, fb * 9));
-  c->mix_bytes = fb * 9;
-  CK(cudaMemsetAsync(c->mix_slab, 0, fb * 9, c->stream));
+  const int nf = c->g.precond == TL_PREC_JAC_DIAG ? 11 : 9;  // + the FP32 Mi and z for jac_diag
+  CK(cudaMalloc(&c->mix_slab, fb * nf));
+  c->mix_bytes = fb * nf;
+  CK(cudaMemsetAsync(c->mix_slab, 0, fb * nf, c->stream));
   float* b = reinterpret_cast<float*>(c->mix_slab);
   const size_t step = fb / sizeof(float);
   c->mix = MixFields{b,            b + step,     b + 2 * step, b + 3 * step, b + 4 * step,
-                     b + 5 * step, b + 6 * step, b + 7 * step, b + 8 * step, c->counter + MIX_ERR_WORD};
+                     b + 5 * step, b + 6 * step, b + 7 * step, b + 8 * step, c->counter + MIX_ERR_WORD,
+                     nf == 11 ? b + 9 * step : nullptr, nf == 11 ? b + 10 * step : nullptr};
   CK(cudaMalloc(&c->mst, sizeof(MixState)));
   CK(cudaMallocHost(&c->mst_host, sizeof(MixState)));
   if (prepare_mix_kernels() != 0) return fail(TL_ERR_CUDA, "cannot set the mixed-precision kernels' shared memory");
@@ -1224,7 +1226,7 @@ int mix_restart(tl_ctx* c, const Reduce& rd, double* floor_est) {
   if ((rc = check_launch("mixed restart"))) return rc;
   if ((rc = sync_mix(c))) return rc;
   *floor_est = DBL_EPSILON * std::sqrt(H.trial_scale);
-  H.rro = H.rr = H.rr_max = H.trial_rr32;
+  H.rro = H.rr = H.rr_max = H.trial_rz32;
   H.p_pending = 0;
   H.status = RUN;
   return TL_OK;
@@ -1268,13 +1270,16 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
   launch_mix_trial(c->f, c->mix, c->L, rd, c->mst, true, c->stream);  // r = p = u0 - A u
   if ((rc = check_launch("mixed set-up"))) return rc;
   if ((rc = sync_mix(c))) return rc;
+  // initial residual: the 2-norm of r as the reference's calc_2norm gives it; the loop's error
+  // is sqrt(r.z) (= that norm without a preconditioner; tea_solve.f90:124-130,402-410)
   const double initial_residual = std::sqrt(std::fabs(H.trial_rr));
-  H.rro = H.rr = H.rr_max = H.trial_rr32;
+  H.rro = H.rr = H.rr_max = H.trial_rz32;
   H.n = 1;
   H.p_pending = 0;
   H.d_pending = 0;
-  H.status = (H.trial_rr32 > 0.0 && std::isfinite(H.trial_rr32)) ? RUN : EXIT_CONVERGED;
-  double res = initial_residual, prev = initial_residual;
+  H.status = (H.trial_rz32 > 0.0 && std::isfinite(H.trial_rz32)) ? RUN : EXIT_CONVERGED;
+  double res = std::sqrt(std::fabs(H.trial_rz)), prev = res;
+  double true_res = initial_residual;  // ||u0 - A u||, the rounding-floor test's measure
   double floor_est = DBL_EPSILON * std::sqrt(H.trial_scale);
   int outer = 0, stalled = 0, stop = TL_STOP_EPS;
   bool rejected = false, stall_restarted = false;
@@ -1284,7 +1289,7 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
       stop = TL_STOP_EPS;
       break;
     }
-    if (res <= TL_FLOOR_FACTOR * floor_est) {  // no correction can lower it much further
+    if (true_res <= TL_FLOOR_FACTOR * floor_est) {  // no correction can lower it much further
       stop = TL_STOP_FLOOR;
       break;
     }
@@ -1326,7 +1331,7 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
     launch_mix_trial(c->f, c->mix, c->L, rd, c->mst, false, c->stream);
     if ((rc = check_launch("mixed trial residual"))) return rc;
     if ((rc = sync_mix(c))) return rc;
-    const double res_t = std::sqrt(std::fabs(H.trial_rr));
+    const double res_t = std::sqrt(std::fabs(H.trial_rz));
     if (!std::isfinite(res_t)) return fail(TL_ERR_BREAKDOWN, "tl_tea_leaf: non-finite residual");
     if (switching && !(res_t < prev)) {
       CK(cudaMemsetAsync(c->mix.d, 0, fbytes, c->stream));  // keep u, drop the correction
@@ -1355,6 +1360,7 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
     stalled = (res_t > 0.9 * prev) ? stalled + 1 : 0;
     if (stalled == 0) stall_restarted = false;
     res = prev = res_t;
+    true_res = std::sqrt(std::fabs(H.trial_rr));
     if (switching) {
       pre->switched = true;
       break;
@@ -1374,9 +1380,9 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
       continue;
     }
     // continue the CG process with r replaced by the true residual, search direction kept
-    H.beta = H.trial_rr32 / H.rro_prev;
+    H.beta = H.trial_rz32 / H.rro_prev;
     if (H.hist_b) CK(cudaMemcpyAsync(H.hist_b + (H.n - 1), &H.beta, sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    H.rro = H.rr = H.rr_max = H.trial_rr32;
+    H.rro = H.rr = H.rr_max = H.trial_rz32;
     H.p_pending = 1;
     H.status = RUN;
   }
@@ -1403,8 +1409,8 @@ int mixed_cg(tl_ctx* c, const tl_solve_opts* o, tl_solve_info* info, long long l
   info->cg_calc_steps = inner_total;
   info->initial_residual = initial_residual;
   info->error = res;
-  info->exact_error = res;
-  info->true_residual = res;
+  info->exact_error = true_res;
+  info->true_residual = true_res;
   info->residual_floor = floor_est;
   info->stop_reason = stop;
   info->outer_iterations = outer;
@@ -1585,9 +1591,12 @@ int check_opts(const tl_ctx* c, const tl_solve_opts* o) {
   if (o->max_iters < 1) return fail(TL_ERR_ARG, "tl_tea_leaf: max_iters must be >= 1");
   if (o->precision != TL_PRECISION_FP64 && o->precision != TL_PRECISION_MIXED)
     return fail(TL_ERR_ARG, "tl_tea_leaf: unknown precision form");
-  if (o->precision == TL_PRECISION_MIXED && (o->solver == TL_SOLVER_JACOBI || c->g.precond != TL_PREC_NONE))
+  if (o->precision == TL_PRECISION_MIXED &&
+      (o->solver == TL_SOLVER_JACOBI || c->g.precond == TL_PREC_JAC_BLOCK ||
+       (c->g.precond == TL_PREC_JAC_DIAG && o->solver != TL_SOLVER_CG)))
     return fail(TL_ERR_ARG,
-                "tl_tea_leaf: the mixed-precision form is implemented for CG, Chebyshev and PPCG without preconditioner");
+                "tl_tea_leaf: the mixed-precision form is implemented for CG (no preconditioner or jac_diag), "
+                "Chebyshev and PPCG (no preconditioner)");
   return TL_OK;
 }
 

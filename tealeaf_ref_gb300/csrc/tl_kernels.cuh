@@ -121,6 +121,8 @@ struct MixFields {
   float *r, *p, *p2, *w, *d;
   float* e;             // second buffer of the blocked polynomial sweeps' ping-pong
   unsigned* err;        // set by a blocked sweep whose bounded wait for a staged row expired
+  float* mi;            // FP32 copy of the jac_diag preconditioner Mi = 1/Di (null: no preconditioner)
+  float* z;             // jac_diag: z = Mi r of the FP32 CG process (null: no preconditioner)
 };
 struct MixState {
   double rro, rro_prev, pw, rr, alpha, beta;  // FP32-vector CG scalars (FP64)
@@ -129,6 +131,9 @@ struct MixState {
   double trial_rr;                            // ||u0 - A (u + d)||^2 in FP64 (last trial)
   double trial_rr32;                          // r.r of its FP32 rounding
   double trial_scale;                         // sum of (|u0| + |Di u| + sum |c u_nb|)^2 (last trial)
+  double trial_rz;                            // r.(Mi r) in FP64 of the last trial (= trial_rr without
+                                              // a preconditioner): the reference's error norm
+  double trial_rz32;                          // r32.(Mi32 r32) of its FP32 rounding (the FP32 process's r.z)
   double d_alpha;
   int n, max_n, phase_end, status, p_pending, d_pending, d_psel;
   // CG presteps of the mixed Chebyshev form: stop with STOP_SWITCH once step n >= presteps

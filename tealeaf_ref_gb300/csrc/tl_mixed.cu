@@ -14,6 +14,12 @@
 // true residual satisfies the reference's test sqrt(r.r) < eps * initial residual
 // (tea_solve.f90:410) or stops falling (the FP64 accuracy floor of u0 - A u).
 //
+// With the jac_diag preconditioner (MixFields::mi non-null) the FP32 process is preconditioned
+// CG: the update sweep (and a trial) also writes z = Mi32 r (Mi32 = the FP32 rounding of the
+// FP64 Mi = 1/Di) and reduces r.z; the matvec sweep stages z in place of r for p = z + beta p.
+// The trial residual also reduces r.(Mi r) in FP64, the norm the reference's preconditioned CG
+// tests (error = rrn = r.z, tea_leaf_cg_kernel.f90:256-283).
+//
 // The FP32 sweeps are the FP64 fused CG sweeps (tl_fused.cu) on float data: p update +
 // 5-point matvec + p.w with the deferred d += alpha p, and r -= alpha w + r.r.  They move 48
 // bytes per cell-iteration and do no FP64 arithmetic per cell: the dot products are summed
@@ -64,10 +70,12 @@ __device__ __forceinline__ void mix_finish(MixState* ms) {
 // The pending d update was flushed before the trial (k_mix_flush_d), so it is cleared here.
 struct EpiMixTrial {
   MixState* ms;
-  __device__ void operator()(double (&acc)[3]) const {
+  __device__ void operator()(double (&acc)[5]) const {
     ms->trial_rr = acc[0];
     ms->trial_rr32 = acc[1];
     ms->trial_scale = acc[2];
+    ms->trial_rz = acc[3];
+    ms->trial_rz32 = acc[4];
     ms->d_pending = 0;
   }
 };
@@ -105,7 +113,7 @@ struct EpiMixUr {
   }
 };
 
-// FP32 copies of the pre-scaled face coefficients and the diagonal.
+// FP32 copies of the pre-scaled face coefficients, the diagonal and the jac_diag Mi.
 __global__ void k_mix_prep(Fields f, MixFields m, Layout L) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   for (int k = blockIdx.y + 1; k <= L.ny + 1; k += gridDim.y) {
@@ -113,7 +121,10 @@ __global__ void k_mix_prep(Fields f, MixFields m, Layout L) {
     const long long c = L.at(j, k);
     m.cx[c] = (float)f.cx[c];
     m.cy[c] = (float)f.cy[c];
-    if (j <= L.nx && k <= L.ny) m.di[c] = (float)f.di[c];
+    if (j <= L.nx && k <= L.ny) {
+      m.di[c] = (float)f.di[c];
+      if (m.mi) m.mi[c] = (float)f.mi[c];
+    }
   }
 }
 
@@ -123,14 +134,16 @@ __global__ void k_mix_prep(Fields f, MixFields m, Layout L) {
 // squared norm of the per-cell magnitude sum |u0| + |Di u| + sum |c u_nb|: FP64 rounding of u
 // and of the residual arithmetic leaves r uncertain by a small multiple of eps_64 times it,
 // the level below which no correction can lower the true residual.
-// first: the start of the CG process, p32 = r32 in the buffer the next k_mix_w reads as its
-// previous direction.  mirror = false: off-domain neighbours are read from the halo cells as
+// With jac_diag also r.(Mi r) and r32.(Mi32 r32).
+// first: the start of the CG process, p32 = r32 (z32 = Mi32 r32 with jac_diag) in the buffer the
+// next k_mix_w reads as its previous direction.  mirror = false: off-domain neighbours are read from the halo cells as
 // they are (u's halo as last exchanged, d's halo zero) -- the operator the reference's
 // Chebyshev iteration applies, whose u halo is not exchanged after the switch
 // (tea_solve.f90:246-250).
 __global__ void k_mix_trial(Fields f, MixFields m, Layout L, Reduce rd, MixState* ms, bool first, bool mirror) {
-  double acc[3] = {0.0, 0.0, 0.0};
+  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   float* __restrict__ p0 = (ms->n & 1) ? m.p : m.p2;
+  const float* __restrict__ mi32 = m.mi;
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
     if (j > L.nx) continue;
@@ -149,13 +162,25 @@ __global__ void k_mix_trial(Fields f, MixFields m, Layout L, Reduce rd, MixState
     acc[0] = fma(r, r, acc[0]);
     const float r32 = (float)r;
     m.r[c] = r32;
-    if (first) p0[c] = r32;
     acc[1] = fma((double)r32, (double)r32, acc[1]);
+    if (mi32) {
+      const float z32 = mi32[c] * r32;
+      m.z[c] = z32;
+      if (first) p0[c] = z32;
+      acc[3] = fma(r, f.mi[c] * r, acc[3]);
+      acc[4] = fma((double)r32, (double)z32, acc[4]);
+    } else if (first) {
+      p0[c] = r32;
+    }
     const double s = fabs(f.u0[c]) + fabs(f.di[c] * uc) + fabs(f.cy[c + L.ld] * ut) + fabs(f.cy[c] * ub) +
                      fabs(f.cx[c + 1] * ur) + fabs(f.cx[c] * ul);
     acc[2] = fma(s, s, acc[2]);
   }
-  grid_reduce<3>(acc, rd, EpiMixTrial{ms});
+  if (!mi32) {
+    acc[3] = acc[0];
+    acc[4] = acc[1];
+  }
+  grid_reduce<5>(acc, rd, EpiMixTrial{ms});
 }
 
 
@@ -197,7 +222,8 @@ __device__ __forceinline__ void mix_commit() { asm volatile("cp.async.commit_gro
 template <int N>
 __device__ __forceinline__ void mix_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N)); }
 
-// p_n = r + beta p_{n-1} (FP32), w = A p_n (FP32), p.w (Dot2), deferred d += alpha p_{n-1}.
+// p_n = r + beta p_{n-1} (z in place of r with jac_diag; FP32), w = A p_n (FP32), p.w (Dot2),
+// deferred d += alpha p_{n-1}.
 // Same row march as the FP64 sweep (tl_fused.cu), four columns per thread, with the inputs of
 // row k+1+MP staged while row k is computed.
 __global__ void __launch_bounds__(MT) k_mix_w(MixFields m, Layout L, Reduce rd, MixState* ms, int rows_per_cta) {
@@ -209,7 +235,7 @@ __global__ void __launch_bounds__(MT) k_mix_w(MixFields m, Layout L, Reduce rd, 
   const float da = (float)ms->d_alpha;
   const float* __restrict__ pold = (n & 1) ? m.p : m.p2;
   float* __restrict__ pout = (n & 1) ? m.p2 : m.p;
-  const float* __restrict__ r = m.r;
+  const float* __restrict__ r = m.mi ? m.z : m.r;  // the source of the p update: z with jac_diag
   extern __shared__ __align__(16) float mix_smem[];
   float(*buf)[MSW + 2] = reinterpret_cast<float(*)[MSW + 2]>(mix_smem + MNS * MARR * MRW);
   const int t = threadIdx.x;
@@ -361,7 +387,9 @@ __global__ void __launch_bounds__(MT) k_mix_w(MixFields m, Layout L, Reduce rd, 
   grid_reduce<1>(acc, rd, EpiMixW{ms});
 }
 
-// r -= alpha w (FP32), r.r (Dot2), inner epilogue.  Four columns per thread.
+// r -= alpha w (FP32), r.r (Dot2; with jac_diag z = Mi32 r written and r.z), inner epilogue.
+// Four columns per thread.
+template <bool PRE>
 __global__ void __launch_bounds__(MT) k_mix_ur(MixFields m, Layout L, Reduce rd, MixState* ms) {
   if (ms->status != RUN) return;
   const float alpha = (float)ms->alpha;
@@ -372,13 +400,14 @@ __global__ void __launch_bounds__(MT) k_mix_ur(MixFields m, Layout L, Reduce rd,
     // four rows per pass with every load issued before any use (memory-level parallelism)
     const int gy = gridDim.y;
     for (int k = blockIdx.y + 1; k <= L.ny; k += 4 * gy) {
-      F4 ww[4], rr[4];
+      F4 ww[4], rr[4], mm[PRE ? 4 : 1];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         if (k + u * gy <= L.ny) {
           const long long c = L.at(ja, k + u * gy);
           ww[u].load(m.w, c);
           rr[u].load(m.r, c);
+          if constexpr (PRE) mm[u].load(m.mi, c);
         }
       }
 #pragma unroll
@@ -387,8 +416,14 @@ __global__ void __launch_bounds__(MT) k_mix_ur(MixFields m, Layout L, Reduce rd,
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             rr[u].v[i] = fmaf(-alpha, ww[u].v[i], rr[u].v[i]);
-            if (i < nv) dot.add(rr[u].v[i], rr[u].v[i]);
+            if constexpr (PRE) {
+              mm[u].v[i] *= rr[u].v[i];  // z = Mi32 r
+              if (i < nv) dot.add(rr[u].v[i], mm[u].v[i]);
+            } else {
+              if (i < nv) dot.add(rr[u].v[i], rr[u].v[i]);
+            }
           }
+          if constexpr (PRE) mm[u].store(m.z, L.at(ja, k + u * gy), nv);
           rr[u].store(m.r, L.at(ja, k + u * gy), nv);
         }
       }
@@ -468,7 +503,10 @@ void launch_mix_iteration(const MixFields& m, const Layout& L, const Reduce& rd,
   int gy = (2048 + ns - 1) / ns;
   if (gy > L.ny) gy = L.ny;
   if ((long long)gy * ns > MAX_REDUCE_BLOCKS) gy = MAX_REDUCE_BLOCKS / ns;
-  { ++launch_counter(); k_mix_ur<<<dim3(ns, gy), MT, 0, s>>>(m, L, rd, ms); }
+  if (m.mi)
+    { ++launch_counter(); k_mix_ur<true><<<dim3(ns, gy), MT, 0, s>>>(m, L, rd, ms); }
+  else
+    { ++launch_counter(); k_mix_ur<false><<<dim3(ns, gy), MT, 0, s>>>(m, L, rd, ms); }
 }
 
 void launch_mix_apply(const Fields& f, const MixFields& m, const Layout& L, cudaStream_t s) {

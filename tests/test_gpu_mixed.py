@@ -19,6 +19,9 @@ CASES = [
     dict(coefficient=1),
     dict(reflective=True),
     dict(nx=200, ny=131, n_rect=6, n_circ=3),
+    dict(precond="jac_diag"),
+    dict(precond="jac_diag", reflective=True, nx=200, ny=131),
+    dict(precond="jac_diag", nx=1030, ny=700, steps=2),
 ]
 
 
@@ -138,7 +141,8 @@ def test_mixed_ppcg_reference_deck(golden):
 def test_mixed_rejected_for_jacobi_and_preconditioners():
     from tealeaf_ref_gb300 import native
 
-    for kw in (dict(solver="jacobi"), dict(solver="cg", precond="jac_diag"),
+    for kw in (dict(solver="jacobi"), dict(solver="cg", precond="jac_block"),
+               dict(solver="chebyshev", precond="jac_diag"), dict(solver="ppcg", ppcg_inner_steps=4, precond="jac_diag"),
                dict(solver="ppcg", ppcg_inner_steps=4, precond="jac_block")):
         d = small_deck(nx=16, ny=16, **kw)
         with native.Chunk.from_deck(d) as c:

@@ -107,6 +107,10 @@ def parse(argv=None):
                     help="instead of the CG line: the adjoint problem (2048^2, 10 steps; gradient of "
                          "sum (u - u_target)^2 wrt density), forward + reverse time and finite-difference checks")
     ap.add_argument("--fd-cells", type=int, default=16, help="adjoint: cells for the per-cell difference check")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="cg line: skip the compact measurements of the other workloads (Jacobi / Chebyshev / "
+                         "PPCG at 4096^2 with their CPU baselines, the Chebyshev / PPCG time to solution in both "
+                         "forms, the 2048^2 adjoint)")
     ap.add_argument("--compare-fp64", action="store_true",
                     help="chebyshev / ppcg: also solve the first time step from the generated state to tl_eps "
                          "in the FP64 and the mixed form and report time, true residual and their differences")
@@ -480,6 +484,101 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def compact_line(solver, steps=5, warmup=2, cpu_steps=1):
+    """A compact measurement of one 4096^2 solver line (device-timed steps with the line's kernel
+    timer, its roofline figure and the CPU port on the same window), for the record of the
+    headline run."""
+    from tealeaf_ref_gb300 import native
+
+    a = parse(["--solver", solver, "--steps", str(steps), "--warmup", str(warmup)])
+    d = workload(a)
+    opts = native.opts_from_deck(d)
+    dt = d.initial_timestep
+    cells = a.cells * a.cells
+    timer, kernel_text, kbytes, kops = KERNELS[solver]
+    with native.Chunk.from_deck(d) as c:
+        for _ in range(warmup):
+            c.tea_leaf(opts, dt)
+        c.profile(True)
+        infos = [c.tea_leaf(opts, dt) for _ in range(steps)]
+        k_ms, k_n = c.profile_read(timer)
+        c.profile(False)
+        dens, ener = c.download("density"), c.download("energy1")
+    dev_s = sum(i.solve_seconds for i in infos)
+    its = sum(min(i.n_exit, a.iters) for i in infos)
+    peak, _ = measured_peaks()
+    t_launch = k_ms / k_n * 1e-3 if k_n else None
+    out = {"metric": metric_name(a), "value": cells * its / dev_s, "unit": "cell-iterations/s",
+           "ms_per_step": 1e3 * dev_s / steps, "steps": steps, "warmup": warmup, "config": config_json(a, 1),
+           "roofline": {"kernel": kernel_text, "algorithmic_bytes_per_cell": kbytes,
+                        "launch_ms": k_ms / k_n if k_n else None,
+                        "achieved_gbs": kbytes * cells / t_launch / 1e9 if t_launch else None,
+                        "frac": kbytes * cells / t_launch / 1e9 / peak if t_launch else None}}
+    try:
+        total, cits, cores = cpu_port_steps(d, a.cpu_iters, cpu_steps, 1, dens, ener)
+        out["cpu_baseline"] = {"value": cells * cits / total, "unit": "cell-iterations/s", "cores": cores,
+                               "kind": "port", "sample": cpu_sample_text(a, cpu_steps, a.cpu_iters)}
+    except Exception as e:  # the baseline is reported, never required
+        out["cpu_baseline"] = {"value": None, "sample": "failed: %s" % e}
+    return out
+
+
+def adjoint_timing():
+    """The 2048^2 adjoint problem's forward and reverse times and its directional
+    finite-difference check (the per-cell checks: --adjoint)."""
+    import numpy as np
+
+    from tealeaf_ref_gb300 import deck as dk
+    from tealeaf_ref_gb300 import native
+    from tealeaf_ref_gb300.adjoint import forward_loss, perturbed_density, squared_error_gradient
+
+    d = dk.config_deck(4)
+    T, dt = d.end_step, d.initial_timestep
+    opts = native.opts_from_deck(d)
+    with native.Chunk.from_deck(d) as c:
+        rho, e0 = c.download("density"), c.download("energy1")
+        forward_loss(c, perturbed_density(rho, 4), e0, np.zeros_like(rho), opts, dt, T)
+        target = c.download("u")
+        t0 = time.perf_counter()
+        forward_loss(c, rho, e0, target, opts, dt, T)
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        loss, g, _, rinfo = squared_error_gradient(c, rho, e0, target, opts, dt, T, rho_only=True)
+        t_both = time.perf_counter() - t0
+        rng = np.random.Generator(np.random.PCG64(4))
+        v = rho * rng.choice([-1.0, 1.0], size=rho.shape)
+        h = 1e-5
+        fd = (forward_loss(c, rho + h * v, e0, target, opts, dt, T) -
+              forward_loss(c, rho - h * v, e0, target, opts, dt, T)) / (2 * h)
+        gd = float(np.sum(g * v))
+    return {"workload": "adjoint problem: 2048x2048 cells, 8 rectangles (seed 4), 10 FP64 CG steps, loss "
+                        "sum (u - u_target)^2, gradient wrt density",
+            "forward_s": t_fwd, "forward_and_reverse_s": t_both, "reverse_s": t_both - t_fwd,
+            "reverse_cg_iterations": rinfo.reported_iterations,
+            "fd_directional": {"h": h, "fd": fd, "adjoint": gd, "rel_err": abs(fd - gd) / abs(gd)}}
+
+
+def other_workloads():
+    """The record of every other workload, measured after the headline (rank 0, one GPU)."""
+    out = {}
+    for s in ("jacobi", "chebyshev", "ppcg"):
+        try:
+            out[s] = compact_line(s)
+        except Exception as e:
+            out[s] = {"failed": str(e)}
+    for s in ("ppcg", "chebyshev"):
+        try:
+            a = parse(["--solver", s])
+            out["%s_time_to_solution" % s] = solve_time_to_solution(workload(a), a)
+        except Exception as e:
+            out["%s_time_to_solution" % s] = {"failed": str(e)}
+    try:
+        out["adjoint"] = adjoint_timing()
+    except Exception as e:
+        out["adjoint"] = {"failed": str(e)}
+    return out
+
+
 def e2e_legs(chunk, opts, dt, args, grp, cells):
     """End to end through the C ABI with pinned host buffers.  One untimed step of each form
     (synchronous; pipelined) picks the form of the timed steps; the other form is then timed
@@ -693,11 +792,14 @@ def main(argv=None):
             out["ppcg_inner_per_step"] = [i.ppcg_inner_iters for i in infos]
         if extra:
             out[extra[0]] = extra[1]
-        print(json.dumps(out), flush=True)
     if pins:
         for p in pins:
             p.close()
     chunk.close()
+    if rank == 0:
+        if world == 1 and args.solver == "cg" and args.precision == "fp64" and not args.no_workloads:
+            out["other_workloads"] = other_workloads()
+        print(json.dumps(out), flush=True)
     grp.close()
 
 

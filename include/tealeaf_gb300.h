@@ -83,8 +83,8 @@ typedef struct tl_solve_opts {
   int ppcg_inner_steps;  /* tl_ppcg_inner_steps (after the PPCG default) */
   int check_result;      /* tl_check_result */
   /* Precision form (no reference counterpart): TL_PRECISION_FP64 runs the reference's
-   * algorithm in FP64.  TL_PRECISION_MIXED (CG without a preconditioner or with jac_diag;
-   * Chebyshev and PPCG without a preconditioner):
+   * algorithm in FP64.  TL_PRECISION_MIXED (CG, Chebyshev and PPCG, without a preconditioner
+   * or with jac_diag):
    * CG runs on FP32 vectors and FP32 copies of the operator (and of Mi), with FP64 reductions
    * and step coefficients, the solution accumulated in FP64 and the residual periodically
    * replaced by the FP64 true residual u0 - A u (the search direction is kept across replacements);

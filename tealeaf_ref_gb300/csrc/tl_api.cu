@@ -1591,12 +1591,10 @@ int check_opts(const tl_ctx* c, const tl_solve_opts* o) {
   if (o->max_iters < 1) return fail(TL_ERR_ARG, "tl_tea_leaf: max_iters must be >= 1");
   if (o->precision != TL_PRECISION_FP64 && o->precision != TL_PRECISION_MIXED)
     return fail(TL_ERR_ARG, "tl_tea_leaf: unknown precision form");
-  if (o->precision == TL_PRECISION_MIXED &&
-      (o->solver == TL_SOLVER_JACOBI || c->g.precond == TL_PREC_JAC_BLOCK ||
-       (c->g.precond == TL_PREC_JAC_DIAG && o->solver != TL_SOLVER_CG)))
+  if (o->precision == TL_PRECISION_MIXED && (o->solver == TL_SOLVER_JACOBI || c->g.precond == TL_PREC_JAC_BLOCK))
     return fail(TL_ERR_ARG,
-                "tl_tea_leaf: the mixed-precision form is implemented for CG (no preconditioner or jac_diag), "
-                "Chebyshev and PPCG (no preconditioner)");
+                "tl_tea_leaf: the mixed-precision form is implemented for CG, Chebyshev and PPCG without a "
+                "preconditioner or with jac_diag");
   return TL_OK;
 }
 

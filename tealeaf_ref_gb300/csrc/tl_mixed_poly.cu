@@ -50,16 +50,19 @@ __device__ __forceinline__ float apply_a32(const float* __restrict__ v, const Mi
   return a;
 }
 
-// tea_leaf_kernel_ppcg_init_sd (tea_leaf_ppcg_kernel.f90:31-88, no preconditioner) in FP32:
-// rtemp = r, sd = r / theta (as r * (1/theta) in FP32: a per-cell FP64 division would make this
-// copy FP64-bound), utemp = sd.
+// The preconditioner's z of a residual value: Mi32 x with jac_diag (m.mi non-null), else x.
+__device__ __forceinline__ float prec32(const MixFields& m, long long c, float x) { return m.mi ? m.mi[c] * x : x; }
+
+// tea_leaf_kernel_ppcg_init_sd (tea_leaf_ppcg_kernel.f90:31-88) in FP32: rtemp = r, sd = z / theta
+// (z = r, or Mi r with jac_diag; as z * (1/theta) in FP32: a per-cell FP64 division would make
+// this copy FP64-bound), utemp = sd.
 __global__ void k_poly_ppcg_init(const double* __restrict__ r, MixFields m, Layout L, float inv_theta) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (j > L.nx) return;
   for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
     const long long c = L.at(j, k);
     const float rv = (float)r[c];
-    const float sd = rv * inv_theta;
+    const float sd = prec32(m, c, rv) * inv_theta;
     m.r[c] = rv;
     m.p[c] = sd;
     m.w[c] = sd;
@@ -67,7 +70,8 @@ __global__ void k_poly_ppcg_init(const double* __restrict__ r, MixFields m, Layo
 }
 
 // One inner step (tea_leaf_kernel_ppcg_inner, ppcg_kernel.f90:204-310) in FP32:
-// rtemp -= A sd; sd' = a sd + b rtemp; utemp += sd'.  z (nullable, FP64): z = utemp after the
+// rtemp -= A sd; sd' = a sd + b rtemp (b Mi rtemp with jac_diag); utemp += sd'.  z (nullable,
+// FP64): z = utemp after the
 // last step (tea_leaf_ppcg_update_z_kernel, :453-477).
 __global__ void k_poly_ppcg_step(MixFields m, const float* __restrict__ sd_in, float* __restrict__ sd_out, Layout L,
                                  float a, float b, double* __restrict__ z) {
@@ -77,7 +81,7 @@ __global__ void k_poly_ppcg_step(MixFields m, const float* __restrict__ sd_in, f
     const long long c = L.at(j, k);
     const float rt = m.r[c] - apply_a32<true>(sd_in, m, c, j, k, L);
     m.r[c] = rt;
-    const float sd = fmaf(a, sd_in[c], b * rt);
+    const float sd = fmaf(a, sd_in[c], b * prec32(m, c, rt));
     sd_out[c] = sd;
     const float ut = m.w[c] + sd;
     m.w[c] = ut;
@@ -96,20 +100,20 @@ __global__ void k_poly_to_z(MixFields m, Layout L, double* __restrict__ z) {
 }
 
 // Chebyshev on A d = r from d = 0 (tea_leaf_kernel_cheby_init, tea_leaf_cheby_kernel.f90:30-109,
-// with u = 0, u0 = r): p = r / theta, d = p.
+// with u = 0, u0 = r): p = z / theta (z = r, or Mi r with jac_diag), d = p.
 __global__ void k_poly_cheby_start(MixFields m, float* __restrict__ d, Layout L, float inv_theta) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (j > L.nx) return;
   for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
     const long long c = L.at(j, k);
-    const float p = m.r[c] * inv_theta;
+    const float p = prec32(m, c, m.r[c]) * inv_theta;
     m.p[c] = p;
     d[c] = p;
   }
 }
 
 // One Chebyshev iteration on the correction (tea_leaf_kernel_cheby_iterate, :111-200):
-// res = r - A d; p = a p + b res; d' = d + p.
+// res = r - A d; p = a p + b res (b Mi res with jac_diag); d' = d + p.
 __global__ void k_poly_cheby_step(MixFields m, const float* __restrict__ d_in, float* __restrict__ d_out, Layout L,
                                   float a, float b) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -117,7 +121,7 @@ __global__ void k_poly_cheby_step(MixFields m, const float* __restrict__ d_in, f
   for (int k = blockIdx.y + 1; k <= L.ny; k += gridDim.y) {
     const long long c = L.at(j, k);
     const float res = m.r[c] - apply_a32<false>(d_in, m, c, j, k, L);
-    const float p = fmaf(a, m.p[c], b * res);
+    const float p = fmaf(a, m.p[c], b * prec32(m, c, res));
     m.p[c] = p;
     d_out[c] = d_in[c] + p;
   }
@@ -149,7 +153,9 @@ __global__ void k_poly_clear(MixFields m, Layout L) {
 // give the bits of S one-step sweeps, whatever CPL.  Traffic per S steps: the state and the
 // coefficients read once (x 32*CPL / output width, for the halo), the state written once.
 // CPL 2 halves the register windows and the shared memory of a warp (more resident warps)
-// for twice the halo overhead of CPL 4; CPL 4 is the faster (see POLY_CPL).
+// for twice the halo overhead of CPL 4; CPL 4 is the faster (see POLY_CPL).  PRE (jac_diag):
+// the preconditioner Mi32 is one more staged coefficient array, applied to the residual of
+// every step (and of the start) as in the one-step kernels.
 constexpr int TB_S = 4;      // steps per sweep at most
 constexpr int TB_HX = 4;     // halo columns on each side of a warp strip
 constexpr int TB_WARPS = 4;  // warps per CTA
@@ -187,7 +193,7 @@ struct PolyArgs {
 
 // Tensor maps (TMA descriptors) of the fields a blocked sweep reads: each a 2-D view
 // (ld x (ny+2)) with a (32*CPL)-element by 1-row box.
-enum { PM_P = 0, PM_P2, PM_R, PM_W, PM_D, PM_E, PM_CX, PM_CY, PM_DI, PM_R64, PM_N };
+enum { PM_P = 0, PM_P2, PM_R, PM_W, PM_D, PM_E, PM_CX, PM_CY, PM_DI, PM_MI, PM_R64, PM_N };
 struct PolyMaps {
   CUtensorMap t[PM_N];
 };
@@ -210,14 +216,17 @@ __device__ __forceinline__ void store_cols(float* __restrict__ p, long long c, c
   }
 }
 
-// Per-warp shared memory of the blocked sweep: a ring of RING coefficient rows (di, cx, cy, and
-// Chebyshev's right-hand side; CP floats per array row) and a ring of TB_P+1 input-state rows.
+// Per-warp shared memory of the blocked sweep: a ring of RING coefficient rows (di, cx, cy,
+// Chebyshev's right-hand side, and Mi with jac_diag; CP floats per array row) and a ring of
+// TB_P+1 input-state rows.
 // With TMA the array rows are 32*CPL floats apart (every TMA destination 128-byte aligned; the
 // lane that reads column j+CPL past its warp's strip is a halo lane) and TB_P+1 mbarriers follow.
-template <int MODE, int S, bool TMA, int CPL>
+enum { CA_DI = 0, CA_CX = 1, CA_CY = 2, CA_RHS = 3 };  // coefficient arrays; Mi follows the last
+template <int MODE, int S, bool TMA, int CPL, bool PRE>
 struct TbSmem {
   static constexpr int SWX = TbGeom<CPL>::SWX;
-  static constexpr int NC = MODE == POLY_PPCG ? 3 : 4;
+  static constexpr int NC = (MODE == POLY_PPCG ? 3 : 4) + (PRE ? 1 : 0);
+  static constexpr int MI = NC - 1;  // Mi's array (PRE only)
   static constexpr int RING = S + 1 + TB_P;
   static constexpr int CP = TMA ? SWX : SWX + 4;                 // floats per coefficient array row
   static constexpr int SSLOT = (MODE == POLY_PPCG ? 3 : 2) * SWX;  // floats (PPCG: or SWX doubles)
@@ -298,10 +307,10 @@ __device__ __forceinline__ void stage_cols_d(double* dst, const double* __restri
   }
 }
 
-template <int MODE, int S, bool TMA, int CPL>
+template <int MODE, int S, bool TMA, int CPL, bool PRE>
 __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __grid_constant__ PolyMaps pm) {
   constexpr bool PPCG = MODE == POLY_PPCG;
-  using SM = TbSmem<MODE, S, TMA, CPL>;
+  using SM = TbSmem<MODE, S, TMA, CPL, PRE>;
   constexpr int NC = SM::NC, RING = SM::RING, CP = SM::CP, SWX = SM::SWX, W = TbGeom<CPL>::W;
   const int lane = threadIdx.x & 31;
   const int task = blockIdx.x * TB_WARPS + (threadIdx.x >> 5);
@@ -345,7 +354,7 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
     if (lane != 0) return;
     constexpr unsigned RB = 4u * SWX;  // bytes of one float row box
     unsigned bytes = 0;
-    if (row <= crow_max) bytes += (row <= L.ny ? (PPCG ? 3 : 4) : 1) * RB;
+    if (row <= crow_max) bytes += (row <= L.ny ? NC : 1) * RB;
     if (row <= srow_max) bytes += a.first ? (PPCG ? 2 * RB : 0) : (PPCG ? 3 : 2) * RB;
     unsigned long long* bar = &bars[ss];
     if (bytes == 0) {
@@ -358,9 +367,10 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
     if (row <= crow_max) {
       tma_row(coef(cs, 2), &pm.t[PM_CY], tmx, row, bar);
       if (row <= L.ny) {
-        tma_row(coef(cs, 0), &pm.t[PM_DI], tmx, row, bar);
-        tma_row(coef(cs, 1), &pm.t[PM_CX], tmx, row, bar);
-        if (!PPCG) tma_row(coef(cs, 3), &pm.t[PM_R], tmx, row, bar);
+        tma_row(coef(cs, CA_DI), &pm.t[PM_DI], tmx, row, bar);
+        tma_row(coef(cs, CA_CX), &pm.t[PM_CX], tmx, row, bar);
+        if (!PPCG) tma_row(coef(cs, CA_RHS), &pm.t[PM_R], tmx, row, bar);
+        if (PRE) tma_row(coef(cs, SM::MI), &pm.t[PM_MI], tmx, row, bar);
       }
     }
     if (row <= srow_max) {
@@ -385,9 +395,10 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
       const long long c = L.at(j, row);
       stage_cols<CPL>(coef(cs, 2) + lc, m.cy + c, j, 1, L.nx);
       if (row <= L.ny) {
-        stage_cols<CPL>(coef(cs, 0) + lc, m.di + c, j, 1, L.nx);
-        stage_cols<CPL>(coef(cs, 1) + lc, m.cx + c, j, 1, L.nx + 1);
-        if (!PPCG) stage_cols<CPL>(coef(cs, 3) + lc, m.r + c, j, 1, L.nx);
+        stage_cols<CPL>(coef(cs, CA_DI) + lc, m.di + c, j, 1, L.nx);
+        stage_cols<CPL>(coef(cs, CA_CX) + lc, m.cx + c, j, 1, L.nx + 1);
+        if (!PPCG) stage_cols<CPL>(coef(cs, CA_RHS) + lc, m.r + c, j, 1, L.nx);
+        if (PRE) stage_cols<CPL>(coef(cs, SM::MI) + lc, m.mi + c, j, 1, L.nx);
       }
     }
     if (row <= srow_max) {
@@ -438,6 +449,7 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
       prefetch_l2(m.cx + c);
       prefetch_l2(m.cy + c);
       if (!PPCG) prefetch_l2(m.r + c);
+      if (PRE) prefetch_l2(m.mi + c);
     }
     if (TMA) {
       // row mm has landed: lane 0 polls (bounded) and tells the warp, so the warp stays
@@ -461,20 +473,21 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
     for (int i = 0; i < CPL; ++i) nx[i] = n1[i] = n2[i] = 0.f;
     if (mm <= srow_max) {
       if (a.first) {
+        const float* rm = coef(cslot, SM::MI) + lc;  // Mi of row mm (PRE)
         if (PPCG) {
           const double* rs = reinterpret_cast<const double*>(state(sslot, 0)) + lc;
 #pragma unroll
           for (int i = 0; i < CPL; ++i) {
             const float rv = (float)rs[i];
             n1[i] = rv;
-            nx[i] = rv * a.inv_theta;
+            nx[i] = (PRE ? rm[i] * rv : rv) * a.inv_theta;
             n2[i] = nx[i];
           }
         } else {
-          const float* rs = coef(cslot, 3) + lc;
+          const float* rs = coef(cslot, CA_RHS) + lc;
 #pragma unroll
           for (int i = 0; i < CPL; ++i) {
-            nx[i] = rs[i] * a.inv_theta;
+            nx[i] = (PRE ? rm[i] * rs[i] : rs[i]) * a.inv_theta;
             n1[i] = nx[i];
           }
         }
@@ -509,18 +522,19 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
         int qs = cslot - t, qs1 = cslot - t + 1;  // slots of rows q and q+1
         if (qs < 0) qs += RING;
         if (qs1 < 0) qs1 += RING;
-        const float* rdi = coef(qs, 0) + lc;
-        const float* rcx = coef(qs, 1) + lc;
-        const float* rcy = coef(qs, 2) + lc;
-        const float* rcy1 = coef(qs1, 2) + lc;
-        float di[CPL], cxv[CPL], cyb[CPL], cyt[CPL], rhs[CPL];
+        const float* rdi = coef(qs, CA_DI) + lc;
+        const float* rcx = coef(qs, CA_CX) + lc;
+        const float* rcy = coef(qs, CA_CY) + lc;
+        const float* rcy1 = coef(qs1, CA_CY) + lc;
+        float di[CPL], cxv[CPL], cyb[CPL], cyt[CPL], rhs[CPL], mi[CPL];
 #pragma unroll
         for (int i = 0; i < CPL; ++i) {
           di[i] = rdi[i];
           cxv[i] = rcx[i];
           cyb[i] = rcy[i];
           cyt[i] = rcy1[i];
-          rhs[i] = PPCG ? 0.f : coef(qs, NC - 1)[lc + i];
+          rhs[i] = PPCG ? 0.f : coef(qs, CA_RHS)[lc + i];
+          mi[i] = PRE ? coef(qs, SM::MI)[lc + i] : 1.f;
         }
         const float cxn = rcx[CPL];                                          // cx at column j+CPL
         const float left = __shfl_up_sync(FULL, X[t - 1][1][CPL - 1], 1);  // column j-1
@@ -543,13 +557,13 @@ __global__ void __launch_bounds__(32 * TB_WARPS) k_poly_tb(PolyArgs a, const __g
           av = fmaf(-cxv[i], vl, av);
           if (PPCG) {
             const float rt = C1[t - 1][0][i] - av;
-            const float sd = fmaf(a.ca[t - 1], vc, a.cb[t - 1] * rt);
+            const float sd = fmaf(a.ca[t - 1], vc, a.cb[t - 1] * (PRE ? mi[i] * rt : rt));
             o1[i] = rt;
             ox[i] = sd;
             o2[i] = C2[t - 1][0][i] + sd;
           } else {
             const float res = rhs[i] - av;
-            const float pn = fmaf(a.ca[t - 1], C1[t - 1][0][i], a.cb[t - 1] * res);
+            const float pn = fmaf(a.ca[t - 1], C1[t - 1][0][i], a.cb[t - 1] * (PRE ? mi[i] * res : res));
             o1[i] = pn;
             ox[i] = vc + pn;
           }
@@ -631,22 +645,23 @@ void tb_tasks(PolyArgs& a, const Layout& L, int cpl, int warps_per_sm) {
   a.ntasks = a.nstrips * ((L.ny + rows - 1) / rows);
 }
 
-template <int MODE, int S, bool TMA, int CPL>
+template <int MODE, int S, bool TMA, int CPL, bool PRE>
 void launch_tb_s(const PolyArgs& a, const PolyMaps& pm, dim3 grid, cudaStream_t s) {
-  constexpr int bytes = TbSmem<MODE, S, TMA, CPL>::BYTES;
+  constexpr int bytes = TbSmem<MODE, S, TMA, CPL, PRE>::BYTES;
   // above the 48 KB default: the attribute is set on the current device before each launch
-  cudaFuncSetAttribute(k_poly_tb<MODE, S, TMA, CPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  k_poly_tb<MODE, S, TMA, CPL><<<grid, 32 * TB_WARPS, bytes, s>>>(a, pm);
+  cudaFuncSetAttribute(k_poly_tb<MODE, S, TMA, CPL, PRE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  k_poly_tb<MODE, S, TMA, CPL, PRE><<<grid, 32 * TB_WARPS, bytes, s>>>(a, pm);
 }
 
 // resident warps per SM of the S = TB_S instance (the one most sweeps use)
-template <int MODE, bool TMA, int CPL>
+template <int MODE, bool TMA, int CPL, bool PRE>
 int tb_resident_warps() {
   static const int w = [] {
-    constexpr int bytes = TbSmem<MODE, TB_S, TMA, CPL>::BYTES;
-    cudaFuncSetAttribute(k_poly_tb<MODE, TB_S, TMA, CPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    constexpr int bytes = TbSmem<MODE, TB_S, TMA, CPL, PRE>::BYTES;
+    cudaFuncSetAttribute(k_poly_tb<MODE, TB_S, TMA, CPL, PRE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_poly_tb<MODE, TB_S, TMA, CPL>, 32 * TB_WARPS, bytes) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_poly_tb<MODE, TB_S, TMA, CPL, PRE>, 32 * TB_WARPS,
+                                                      bytes) !=
             cudaSuccess ||
         per_sm < 1) {
       cudaGetLastError();
@@ -709,7 +724,7 @@ bool tmap_of(const void* base, const Layout& L, bool f64, int box_w, CUtensorMap
 // the maps of every field a blocked sweep may read; false if TMA is off or unavailable
 bool poly_maps(const MixFields& m, const Layout& L, const double* r64, int box_w, PolyMaps* pm) {
   if (!poly_use_tma()) return false;
-  const float* f[PM_R64] = {m.p, m.p2, m.r, m.w, m.d, m.e, m.cx, m.cy, m.di};
+  const float* f[PM_R64] = {m.p, m.p2, m.r, m.w, m.d, m.e, m.cx, m.cy, m.di, m.mi ? m.mi : m.di};
   for (int i = 0; i < PM_R64; ++i)
     if (!tmap_of(f[i], L, false, box_w, &pm->t[i])) return false;
   if (r64) {
@@ -730,14 +745,21 @@ int map_index(const MixFields& m, const float* p) {
   return PM_R;  // (the first sweep reads no state map)
 }
 
-template <int MODE, bool TMA, int CPL>
+template <int MODE, bool TMA, int CPL, bool PRE>
 void launch_tb_cpl(const PolyArgs& a, int steps, const PolyMaps& pm, dim3 grid, cudaStream_t s) {
   switch (steps) {
-    case 1: launch_tb_s<MODE, 1, TMA, CPL>(a, pm, grid, s); break;
-    case 2: launch_tb_s<MODE, 2, TMA, CPL>(a, pm, grid, s); break;
-    case 3: launch_tb_s<MODE, 3, TMA, CPL>(a, pm, grid, s); break;
-    default: launch_tb_s<MODE, 4, TMA, CPL>(a, pm, grid, s); break;
+    case 1: launch_tb_s<MODE, 1, TMA, CPL, PRE>(a, pm, grid, s); break;
+    case 2: launch_tb_s<MODE, 2, TMA, CPL, PRE>(a, pm, grid, s); break;
+    case 3: launch_tb_s<MODE, 3, TMA, CPL, PRE>(a, pm, grid, s); break;
+    default: launch_tb_s<MODE, 4, TMA, CPL, PRE>(a, pm, grid, s); break;
   }
+}
+template <int MODE, bool TMA, int CPL>
+void launch_tb_pre(const PolyArgs& a, int steps, const PolyMaps& pm, dim3 grid, cudaStream_t s) {
+  if (a.m.mi)
+    launch_tb_cpl<MODE, TMA, CPL, true>(a, steps, pm, grid, s);
+  else
+    launch_tb_cpl<MODE, TMA, CPL, false>(a, steps, pm, grid, s);
 }
 
 template <int MODE>
@@ -749,18 +771,22 @@ void launch_tb(PolyArgs a, int steps, bool tma, int cpl, const PolyMaps& pm, cud
   a.hold_row = poly_test_hold() ? 1 + TB_P : -1;  // task 0 starts its march at row 1
   ++launch_counter();
   if (cpl == 4) {
-    if (tma) launch_tb_cpl<MODE, true, 4>(a, steps, pm, grid, s);
-    else launch_tb_cpl<MODE, false, 4>(a, steps, pm, grid, s);
+    if (tma) launch_tb_pre<MODE, true, 4>(a, steps, pm, grid, s);
+    else launch_tb_pre<MODE, false, 4>(a, steps, pm, grid, s);
   } else {
-    if (tma) launch_tb_cpl<MODE, true, 2>(a, steps, pm, grid, s);
-    else launch_tb_cpl<MODE, false, 2>(a, steps, pm, grid, s);
+    if (tma) launch_tb_pre<MODE, true, 2>(a, steps, pm, grid, s);
+    else launch_tb_pre<MODE, false, 2>(a, steps, pm, grid, s);
   }
 }
 
 template <int MODE>
-int tb_warps(bool tma, int cpl) {
-  if (cpl == 4) return tma ? tb_resident_warps<MODE, true, 4>() : tb_resident_warps<MODE, false, 4>();
-  return tma ? tb_resident_warps<MODE, true, 2>() : tb_resident_warps<MODE, false, 2>();
+int tb_warps(bool tma, int cpl, bool pre) {
+  if (pre) {
+    if (cpl == 4) return tma ? tb_resident_warps<MODE, true, 4, true>() : tb_resident_warps<MODE, false, 4, true>();
+    return tma ? tb_resident_warps<MODE, true, 2, true>() : tb_resident_warps<MODE, false, 2, true>();
+  }
+  if (cpl == 4) return tma ? tb_resident_warps<MODE, true, 4, false>() : tb_resident_warps<MODE, false, 4, false>();
+  return tma ? tb_resident_warps<MODE, true, 2, false>() : tb_resident_warps<MODE, false, 2, false>();
 }
 
 }  // namespace
@@ -778,7 +804,7 @@ void launch_poly_ppcg_inner(const Fields& f, const MixFields& m, const Layout& L
     const int cpl = poly_cols();
     PolyMaps pm;
     const bool tma = poly_maps(m, L, f.r, 32 * cpl, &pm);
-    tb_tasks(a, L, cpl, tb_warps<POLY_PPCG>(tma, cpl));
+    tb_tasks(a, L, cpl, tb_warps<POLY_PPCG>(tma, cpl, m.mi != nullptr));
     int done = 0, par = 0;
     while (done < inner_steps) {
       const int st = inner_steps - done < blk ? inner_steps - done : blk;
@@ -829,7 +855,7 @@ void launch_poly_cheby(const MixFields& m, const Layout& L, double theta, int st
     const int cpl = poly_cols();
     PolyMaps pm;
     const bool tma = poly_maps(m, L, nullptr, 32 * cpl, &pm);
-    tb_tasks(a, L, cpl, tb_warps<POLY_CHEBY>(tma, cpl));
+    tb_tasks(a, L, cpl, tb_warps<POLY_CHEBY>(tma, cpl, m.mi != nullptr));
     const int nb = (iters + blk - 1) / blk;
     const float* din = nullptr;
     const float* pin = nullptr;

@@ -94,6 +94,10 @@ POLY_CASES = [
     dict(solver="chebyshev", ch_cg_presteps=20, coefficient=1),
     dict(solver="chebyshev", ch_cg_presteps=20, reflective=True),
     dict(solver="chebyshev", ch_cg_presteps=30, nx=131, ny=77),
+    dict(solver="ppcg", ppcg_inner_steps=10, ch_cg_presteps=20, precond="jac_diag"),
+    dict(solver="ppcg", ppcg_inner_steps=8, ch_cg_presteps=20, precond="jac_diag", reflective=True),
+    dict(solver="chebyshev", ch_cg_presteps=20, precond="jac_diag"),
+    dict(solver="chebyshev", ch_cg_presteps=20, precond="jac_diag", reflective=True),
 ]
 
 
@@ -142,7 +146,6 @@ def test_mixed_rejected_for_jacobi_and_preconditioners():
     from tealeaf_ref_gb300 import native
 
     for kw in (dict(solver="jacobi"), dict(solver="cg", precond="jac_block"),
-               dict(solver="chebyshev", precond="jac_diag"), dict(solver="ppcg", ppcg_inner_steps=4, precond="jac_diag"),
                dict(solver="ppcg", ppcg_inner_steps=4, precond="jac_block")):
         d = small_deck(nx=16, ny=16, **kw)
         with native.Chunk.from_deck(d) as c:
@@ -153,7 +156,8 @@ def test_mixed_rejected_for_jacobi_and_preconditioners():
 
 @pytest.mark.parametrize("solver", ["ppcg", "chebyshev"])
 @pytest.mark.parametrize("reflective", [False, True])
-def test_blocked_poly_sweeps_bitwise(solver, reflective, monkeypatch):
+@pytest.mark.parametrize("precond", ["none", "jac_diag"])
+def test_blocked_poly_sweeps_bitwise(solver, reflective, precond, monkeypatch):
     """The temporally blocked FP32 sweeps (several polynomial steps per pass over the mesh)
     give the bits of the one-step sweeps: same solution and iteration counts for 3 and 4
     steps per sweep, 2 or 4 columns per lane, TMA or cp.async staging, on a mesh whose width
@@ -161,7 +165,7 @@ def test_blocked_poly_sweeps_bitwise(solver, reflective, monkeypatch):
     from tealeaf_ref_gb300 import native
 
     d = small_deck(nx=301, ny=133, steps=2, n_rect=4, n_circ=2, solver=solver, ppcg_inner_steps=10,
-                   ch_cg_presteps=20, reflective=reflective, max_iters=20000)
+                   ch_cg_presteps=20, reflective=reflective, max_iters=20000, precond=precond)
     opts = native.opts_from_deck(d, precision="mixed")
     runs = []
     # steps per sweep x columns per lane of the warp strips (2 or 4) x staging (TMA or cp.async)

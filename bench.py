@@ -65,7 +65,8 @@ FALLBACK_HBM_GBS = 6800.0
 #  chebyshev u, u0, p, Kx, Ky read; p, u written; A u 5, r 1, p 2, u 1
 #  ppcg      sd, rtemp, utemp, Kx, Ky read; sd, rtemp, utemp written; A sd 5, rtemp 1, sd 2, utemp 1
 KERNELS = {
-    "cg": ("cg_matvec", "k_fused_cg_w (p = r + beta p, w = A p, p.w, deferred u += alpha p)", 64, 8),
+    "cg": ("cg_matvec", "k_fused_cg_ws (p = r + beta p, w = A p, p.w, deferred u += alpha p; input rows staged "
+                        "one row ahead in shared memory)", 64, 8),
     "jacobi": ("jacobi", "k_fused_jacobi (u = (u0 + neighbour fluxes of un) / denominator, sum |u - un|)", 40, 15),
     "chebyshev": ("cheby_iterate", "FP64 Chebyshev iteration (k_cheby_wr: w = A u, r = u0 - w; k_cheby_iter_pu: "
                                    "p = a p + b r, u += p)", 56, 9),

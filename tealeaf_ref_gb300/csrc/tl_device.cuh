@@ -142,9 +142,10 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* scratch) {
 // that arrives last sums all partials in block order (thread t takes t, t+T, ...; then a
 // fixed tree), runs epi(total) in thread 0 and re-arms the ticket.  The result does not
 // depend on which CTA arrives last.
+// scratch: MAX_REDUCE_THREADS * NV doubles of shared memory the block no longer uses otherwise
+// (the caller has synchronised the block after its last use)
 template <int NV, typename Epi>
-__device__ __forceinline__ void grid_reduce(double (&v)[NV], const Reduce& rd, Epi epi) {
-  __shared__ double scratch[MAX_REDUCE_THREADS * NV];
+__device__ __forceinline__ void grid_reduce_in(double (&v)[NV], const Reduce& rd, Epi epi, double* scratch) {
   __shared__ int is_last;
   block_sum<NV>(v, scratch);
   const unsigned nblk = gridDim.x * gridDim.y;
@@ -172,6 +173,12 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NV], const Reduce& rd, E
     *rd.counter = 0u;
     __threadfence();
   }
+}
+
+template <int NV, typename Epi>
+__device__ __forceinline__ void grid_reduce(double (&v)[NV], const Reduce& rd, Epi epi) {
+  __shared__ double scratch[MAX_REDUCE_THREADS * NV];
+  grid_reduce_in<NV>(v, rd, epi, scratch);
 }
 
 }  // namespace tl

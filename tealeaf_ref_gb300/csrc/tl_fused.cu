@@ -20,7 +20,8 @@
 // row k through shared memory for the horizontal neighbours; the two strip-edge columns
 // and the first/last row of a CTA are recomputed (p = src + beta*p costs one FMA).  Off the
 // domain the neighbour is the mirror value (the reference's reflective halo copy of p, or a
-// value multiplied by a zero boundary coefficient otherwise).
+// value multiplied by a zero boundary coefficient otherwise).  The form launched by default,
+// k_fused_cg_ws, stages each row step's inputs into shared memory one row step ahead.
 #include "tl_kernels.cuh"
 
 namespace tl {
@@ -236,6 +237,211 @@ __global__ void __launch_bounds__(FT) k_fused_cg_w(LoopArgs a, int rows_per_cta)
   }
   acc[0] += acc_b;
   grid_reduce<EpiCgW<PPCG>::NV>(acc, a.rd, EpiCgW<PPCG>{a.rd});
+}
+
+// ---- the matvec sweep with its input rows staged one row ahead --------------------------------
+// Same arithmetic, row march and results (bit for bit) as k_fused_cg_w.  The inputs a row step
+// needs -- p_{n-1} and src of row k+1 (with the strip's two halo columns), cy of row k+1, cx,
+// Di and u of row k -- are copied into a two-slot shared-memory ring by
+// asynchronous copies (cp.async) one row step before they are used, so the loads' latency
+// falls under the previous row's arithmetic instead of stalling it.  Every thread stages
+// exactly the columns it reads itself into ring entries no other thread writes (its two
+// columns; the right face cx(j+2) of its second one, which is also the next thread's first
+// column, into an entry of its own; the strip's halo columns in the two edge threads), so the
+// ring needs no barrier: a thread waits only for its own copies (cp.async.wait_group).
+//
+// Unit m of the ring (slot m & 1) holds p_{n-1}, src and cy of row m and cx, Di, u of row
+// m-1; row step k consumes unit k+1 and stages unit k+2 into the slot unit k left.  At 8192^2
+// the sweep takes 1.002 ms per launch against 1.026 ms with direct loads (7 CTAs per SM
+// instead of 9: the ring's 26 KB per CTA bound them; the block sum at the end reuses the ring
+// as its scratch); staging all but u took 1.013 ms.
+constexpr int SROW = SW + 4;  // doubles per staged array row; column col at index col - js + 2
+constexpr int STAGE_ARRAYS = 6;
+constexpr int SSLOT = STAGE_ARRAYS * SROW + FT;  // doubles per slot: the arrays, then cx(j+2) per thread
+constexpr size_t STAGE_SMEM = (size_t)2 * SSLOT * sizeof(double);
+
+__device__ __forceinline__ void cp16(double* dst, const double* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src));
+}
+__device__ __forceinline__ void cp8(double* dst, const double* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src));
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+template <bool PPCG>
+__global__ void __launch_bounds__(FT) k_fused_cg_ws(LoopArgs a, int rows_per_cta) {
+  LoopState* st = a.rd.st;
+  if (st->status != RUN) return;
+  const Layout L = a.L;
+  const int n = st->n;
+  const bool use_z = PPCG || a.precond != 1;
+  const double* __restrict__ src = use_z ? a.f.z : a.f.r;
+  const double* __restrict__ pold = (n & 1) ? a.f.p : a.f.p2;
+  const double beta = st->beta;
+  const bool upd = st->p_pending != 0;
+  double* __restrict__ pout = (n & 1) ? a.f.p2 : a.f.p;
+  double* __restrict__ w = a.f.w;
+  const double* __restrict__ cx = a.f.cx;
+  const double* __restrict__ cy = a.f.cy;
+  const double* __restrict__ di = a.f.di;
+  const bool upd_u = !PPCG && st->u_pending != 0;
+  const double ua = st->u_alpha;
+  double* __restrict__ u = a.f.u;
+
+  extern __shared__ __align__(16) double ring[];
+  __shared__ double buf[2][SW + 2];
+  enum { A_P = 0, A_S, A_CY, A_CX, A_DI, A_U };
+  auto arr = [&](int m, int a_) { return ring + (m & 1) * SSLOT + a_ * SROW; };
+  auto cxr_at = [&](int m) { return ring + (m & 1) * SSLOT + STAGE_ARRAYS * SROW + threadIdx.x; };
+
+  const int t = threadIdx.x;
+  const int js = blockIdx.x * SW + 1;
+  const int ja = js + 2 * t;
+  const int o = 2 * t + 2;  // this thread's first column in a staged row
+  const bool active = ja <= L.nx;
+  const bool has_b = ja + 1 <= L.nx;
+  const bool left_edge = t == 0 && js > 1;
+  const bool right_edge = t == FT - 1 && js + SW <= L.nx;
+  const int k0 = blockIdx.y * rows_per_cta + 1;
+  const int k1 = min(k0 + rows_per_cta - 1, L.ny);
+  const int ld = L.ld;
+
+  // unit m: the copies this thread needs of it (none past the CTA's last row step)
+  auto stage = [&](int m) {
+    if (m <= k1 + 1) {
+      if (m <= L.ny) {  // p_{n-1}, src of row m (row k+1 of step k = m-1; none above the domain)
+        const long long c = L.at(ja, m);
+        if (active) {
+          cp16(arr(m, A_P) + o, pold + c);
+          if (upd) cp16(arr(m, A_S) + o, src + c);
+        }
+        if (left_edge) {
+          cp8(arr(m, A_P) + 1, pold + L.at(js - 1, m));
+          if (upd) cp8(arr(m, A_S) + 1, src + L.at(js - 1, m));
+        }
+        if (right_edge) {
+          cp8(arr(m, A_P) + SW + 2, pold + L.at(js + SW, m));
+          if (upd) cp8(arr(m, A_S) + SW + 2, src + L.at(js + SW, m));
+        }
+      }
+      if (active) {
+        const long long c = L.at(ja, m - 1);
+        cp16(arr(m, A_CY) + o, cy + c + ld);  // cy of row m: the north face of row m-1
+        cp16(arr(m, A_CX) + o, cx + c);
+        if (has_b) cp8(cxr_at(m), cx + c + 2);
+        cp16(arr(m, A_DI) + o, di + c);
+        if (upd_u) cp16(arr(m, A_U) + o, u + c);
+      }
+    }
+    cp_commit();
+  };
+  auto pnew2 = [&](const double* sp, const double* ss) {
+    double2 q = *reinterpret_cast<const double2*>(sp);
+    if (upd) {
+      const double2 r2 = *reinterpret_cast<const double2*>(ss);
+      q.x = fma(beta, q.x, r2.x);
+      q.y = fma(beta, q.y, r2.y);
+    }
+    return q;
+  };
+  auto pnew1 = [&](const double* sp, const double* ss) { return upd ? fma(beta, *sp, *ss) : *sp; };
+
+  double acc[EpiCgW<PPCG>::NV] = {};
+  double acc_b = 0.0;
+  double2 pm = make_double2(0.0, 0.0), pc = pm, pnx = pm, cyc = pm, oc = pm, onx = pm;
+  double hl = 0.0, hr = 0.0;  // p_n of the strip's halo columns in the current row (edge threads)
+  {
+    PNew pn_{src, pold, beta, upd};
+    if (active) {
+      pc = pn_.pair(L.at(ja, k0), oc);
+      pm = (k0 == 1) ? pc : pn_.pair(L.at(ja, k0 - 1));
+      cyc = *reinterpret_cast<const double2*>(cy + L.at(ja, k0));
+    }
+    if (left_edge) hl = pn_.one(L.at(js - 1, k0));
+    if (right_edge) hr = pn_.one(L.at(js + SW, k0));
+  }
+  stage(k0 + 1);
+  for (int k = k0; k <= k1; ++k) {
+    const int b = k & 1;
+    if (active) {
+      buf[b][2 * t + 1] = pc.x;
+      buf[b][2 * t + 2] = pc.y;
+    }
+    if (left_edge) buf[b][0] = hl;
+    if (right_edge) buf[b][SW + 1] = hr;
+    stage(k + 2);
+    cp_wait<1>();  // unit k+1 has landed
+    const int m = k + 1;
+    if (active) {
+      if (k == L.ny) {
+        pnx = pc;
+      } else {
+        pnx = pnew2(arr(m, A_P) + o, arr(m, A_S) + o);
+        if (k < k1) onx = *reinterpret_cast<const double2*>(arr(m, A_P) + o);
+      }
+    }
+    if (k < L.ny) {
+      if (left_edge) hl = pnew1(arr(m, A_P) + 1, arr(m, A_S) + 1);
+      if (right_edge) hr = pnew1(arr(m, A_P) + SW + 2, arr(m, A_S) + SW + 2);
+    }
+    __syncthreads();
+    if (active) {
+      const long long c = L.at(ja, k);
+      const double2 cyn = *reinterpret_cast<const double2*>(arr(m, A_CY) + o);
+      const double2 cxa = *reinterpret_cast<const double2*>(arr(m, A_CX) + o);
+      const double2 dd = *reinterpret_cast<const double2*>(arr(m, A_DI) + o);
+      const double left_a = (ja == 1) ? pc.x : buf[b][ja - js];
+      const double right_a = has_b ? pc.y : pc.x;
+      double wa = dd.x * pc.x;
+      wa = fma(-cyn.x, pnx.x, wa);
+      wa = fma(-cyc.x, pm.x, wa);
+      wa = fma(-cxa.y, right_a, wa);
+      wa = fma(-cxa.x, left_a, wa);
+      acc[0] = fma(wa, pc.x, acc[0]);
+      if (has_b) {
+        const double cxr = *cxr_at(m);
+        const double right_b = (ja + 1 == L.nx) ? pc.y : buf[b][ja - js + 3];
+        double wb = dd.y * pc.y;
+        wb = fma(-cyn.y, pnx.y, wb);
+        wb = fma(-cyc.y, pm.y, wb);
+        wb = fma(-cxr, right_b, wb);
+        wb = fma(-cxa.y, pc.x, wb);
+        acc_b = fma(wb, pc.y, acc_b);
+        *reinterpret_cast<double2*>(w + c) = make_double2(wa, wb);
+        *reinterpret_cast<double2*>(pout + c) = pc;
+        if (upd_u) {
+          double2 uu = *reinterpret_cast<const double2*>(arr(m, A_U) + o);
+          uu.x = fma(ua, oc.x, uu.x);
+          uu.y = fma(ua, oc.y, uu.y);
+          *reinterpret_cast<double2*>(u + c) = uu;
+        }
+      } else {
+        w[c] = wa;
+        pout[c] = pc.x;
+        if (upd_u) u[c] = fma(ua, oc.x, arr(m, A_U)[o]);
+      }
+      if constexpr (PPCG) {
+        const double2 rr = *reinterpret_cast<const double2*>(a.f.r + c);
+        const double2 zz = *reinterpret_cast<const double2*>(a.f.z + c);
+        a.f.r_store[c] = rr.x;
+        acc[1] = fma(zz.x, rr.x, acc[1]);
+        if (has_b) {
+          a.f.r_store[c + 1] = rr.y;
+          acc[1] = fma(zz.y, rr.y, acc[1]);
+        }
+      }
+      cyc = cyn;
+    }
+    pm = pc;
+    pc = pnx;
+    oc = onx;
+  }
+  cp_wait<0>();
+  acc[0] += acc_b;
+  __syncthreads();  // every thread is done with the ring: it becomes the block sum's scratch
+  grid_reduce_in<EpiCgW<PPCG>::NV>(acc, a.rd, EpiCgW<PPCG>{a.rd}, ring);
 }
 
 // ---- persistent cooperative CG (small meshes) ----------------------------------------------
@@ -598,8 +804,22 @@ long long resident_ctas(const void* kernel, int threads, size_t smem) {
   return (long long)sms * per_sm;
 }
 
+// TL_CG_STAGE=0 selects the matvec sweep with direct loads (same bits as the staged one)
+int cg_stage_mode() {
+  const char* e = getenv("TL_CG_STAGE");
+  return (e && e[0] == '0') ? 0 : 1;
+}
+
+template <bool PPCG>
+const void* cg_w_kernel(int mode) {
+  return mode == 0 ? (const void*)k_fused_cg_w<PPCG> : (const void*)k_fused_cg_ws<PPCG>;
+}
+size_t cg_w_smem(int mode) { return mode == 0 ? 0 : STAGE_SMEM; }
+
+// Co-resident CTAs of the staged sweep.  Both forms size their grid from it, so that they
+// split the p.w sum into the same partials and give the same bits.
 long long cg_w_slots() {
-  static const long long slots = resident_ctas((const void*)k_fused_cg_w<false>, FT, 0);
+  static const long long slots = resident_ctas((const void*)k_fused_cg_ws<false>, FT, STAGE_SMEM);
   return slots;
 }
 
@@ -612,10 +832,12 @@ void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s) {
   const int min_rows = (int)(((long long)a.L.ny * ns + MAX_REDUCE_BLOCKS - 1) / MAX_REDUCE_BLOCKS);
   if (rows < min_rows) rows = min_rows;  // keep the CTA count within the partials buffer
   dim3 grid(ns, (a.L.ny + rows - 1) / rows);
-  if (ppcg)
-    { ++launch_counter(); k_fused_cg_w<true><<<grid, FT, 0, s>>>(a, rows); }
-  else
-    { ++launch_counter(); k_fused_cg_w<false><<<grid, FT, 0, s>>>(a, rows); }
+  const int mode = cg_stage_mode();
+  const void* k = ppcg ? cg_w_kernel<true>(mode) : cg_w_kernel<false>(mode);
+  LoopArgs aa = a;
+  void* args[] = {&aa, &rows};
+  ++launch_counter();
+  cudaLaunchKernel(k, grid, dim3(FT), args, cg_w_smem(mode), s);
 }
 
 int persistent_cg_grid() {

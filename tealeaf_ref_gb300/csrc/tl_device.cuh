@@ -11,7 +11,10 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
+
+#include "tl_fp64emu.cuh"
 
 namespace tl {
 
@@ -42,13 +45,24 @@ struct Fields {
 // correction, q = RN(num y), q + (num - den q) y (P. Markstein, "Computation of elementary
 // functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990): three
 // FP64 operations instead of a division.  kx0/kx1 are Kx(j)/Kx(j+1), ky0/ky1 Ky(k)/Ky(k+1).
+// Bit i of INT computes the i-th of the seven products (kx1 ur, kx0 ul, rx (..), ky1 ut,
+// ky0 ub, ry (..), num y) on the integer pipes (dmul_int: the same bits).
+template <int INT = 0>
 __device__ __forceinline__ double jacobi_cell(double u0, double kx0, double kx1, double ky0, double ky1, double ul,
                                               double ur, double ub, double ut, double den, double y, double rx,
                                               double ry) {
-  const double sx = __dmul_rn(rx, __dadd_rn(__dmul_rn(kx1, ur), __dmul_rn(kx0, ul)));
-  const double sy = __dmul_rn(ry, __dadd_rn(__dmul_rn(ky1, ut), __dmul_rn(ky0, ub)));
+  auto mul = [](auto bit, double a, double b) { return (INT & decltype(bit)::value) ? dmul_int(a, b) : __dmul_rn(a, b); };
+  using B0 = std::integral_constant<int, 1>;
+  using B1 = std::integral_constant<int, 2>;
+  using B2 = std::integral_constant<int, 4>;
+  using B3 = std::integral_constant<int, 8>;
+  using B4 = std::integral_constant<int, 16>;
+  using B5 = std::integral_constant<int, 32>;
+  using B6 = std::integral_constant<int, 64>;
+  const double sx = mul(B2{}, rx, __dadd_rn(mul(B0{}, kx1, ur), mul(B1{}, kx0, ul)));
+  const double sy = mul(B5{}, ry, __dadd_rn(mul(B3{}, ky1, ut), mul(B4{}, ky0, ub)));
   const double num = __dadd_rn(__dadd_rn(u0, sx), sy);
-  const double q = __dmul_rn(num, y);
+  const double q = mul(B6{}, num, y);
   return __fma_rn(__fma_rn(-q, den, num), y, q);
 }
 

@@ -115,6 +115,8 @@ SIGNATURES = {
     "tl_adjoint_record_step": (_I, [_P, C.POINTER(SolveOpts), _D, C.POINTER(SolveInfo)]),
     "tl_adjoint_backward": (_I, [_P, _DP, _DP, _I, _DP, _DP, C.POINTER(SolveInfo)]),
     "tl_adjoint_end": (_I, [_P]),
+    # diagnostic, not in the public header: the integer-pipe FP64 multiply against mul.rn.f64
+    "tl_fp64_emu_check": (_I, [_DP, _DP, C.c_longlong, _DP, _DP]),
     "tl_cg_calc_w_noalloc": (_I, [_I, _I, _I, _P, _P, _P, _P, _P, _D, _D, _DP]),
     "tl_profile": (_I, [_P, _I]),
     "tl_profile_read": (_I, [_P, _I, _DP, C.POINTER(C.c_longlong)]),

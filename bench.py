@@ -56,22 +56,26 @@ FP64_OPS_PER_CLOCK_SM = 2   # FP64 pipe peak that ncu reports for GB300: 2 threa
 FALLBACK_HBM_GBS = 6800.0
 
 # Dominant kernel of each line: timer id (tl_profile), what it is, algorithmic bytes per cell per
-# launch, FP64 operations per cell per launch.
+# launch, FP64 operations per cell per launch, and how many of those issue on the FP64 pipe (the
+# rest are products computed on the integer pipes with the same bits).
 #  cg        fused sweep 1: r, p_old, Kx, Ky, u read; p, w, u written (the u += alpha p of the
 #            previous iteration folded in; Di, stored, is not counted because the reference
-#            recomputes it); p update 1, A p 5, p.w 1, deferred u 1 FP64 operations
+#            recomputes it); p update 1, A p 5, p.w 1, deferred u 1 FP64 operations (Di p on
+#            the integer pipes)
 #  jacobi    u0, un, Kx, Ky read; u written; 15 operations (the reference's bits: every product
-#            and sum rounded separately, the quotient by a corrected reciprocal)
+#            and sum rounded separately, the quotient by a corrected reciprocal; six of the
+#            seven products on the integer pipes)
 #  chebyshev u, u0, p, Kx, Ky read; p, u written; A u 5, r 1, p 2, u 1
 #  ppcg      sd, rtemp, utemp, Kx, Ky read; sd, rtemp, utemp written; A sd 5, rtemp 1, sd 2, utemp 1
 KERNELS = {
     "cg": ("cg_matvec", "k_fused_cg_ws (p = r + beta p, w = A p, p.w, deferred u += alpha p; input rows staged "
-                        "one row ahead in shared memory)", 64, 8),
-    "jacobi": ("jacobi", "k_fused_jacobi (u = (u0 + neighbour fluxes of un) / denominator, sum |u - un|)", 40, 15),
+                        "one row ahead in shared memory; Di p on the integer pipes)", 64, 8, 7),
+    "jacobi": ("jacobi", "k_fused_jacobi (u = (u0 + neighbour fluxes of un) / denominator, sum |u - un|; six "
+                         "products on the integer pipes)", 40, 15, 9),
     "chebyshev": ("cheby_iterate", "FP64 Chebyshev iteration (k_cheby_wr: w = A u, r = u0 - w; k_cheby_iter_pu: "
-                                   "p = a p + b r, u += p)", 56, 9),
+                                   "p = a p + b r, u += p)", 56, 9, 9),
     "ppcg": ("ppcg_inner", "FP64 PPCG inner step (k_ppcg_inner_r: rtemp -= A sd; k_ppcg_inner_s: sd = a sd + b rtemp, "
-                           "utemp += sd)", 64, 9),
+                           "utemp += sd)", 64, 9, 9),
 }
 # The precision form's dominant kernels (FP32 streams, 4 B each): the FP32 CG sweep 1 (r, p_old,
 # Kx, Ky, d read; p, w, d written) and one blocked FP32 polynomial step of Chebyshev (d, r, p, Kx,
@@ -496,7 +500,7 @@ def compact_line(solver, steps=5, warmup=2, cpu_steps=1):
     opts = native.opts_from_deck(d)
     dt = d.initial_timestep
     cells = a.cells * a.cells
-    timer, kernel_text, kbytes, kops = KERNELS[solver]
+    timer, kernel_text, kbytes, kops, _ = KERNELS[solver]
     with native.Chunk.from_deck(d) as c:
         for _ in range(warmup):
             c.tea_leaf(opts, dt)
@@ -680,7 +684,7 @@ def main(argv=None):
     cells = args.cells * args.cells
     if args.precision == "mixed" and args.solver == "jacobi":
         raise SystemExit("the precision form is built for CG, Chebyshev and PPCG")
-    timer, kernel_text, kbytes, kops = KERNELS[args.solver]
+    timer, kernel_text, kbytes, kops, kpipe = KERNELS[args.solver]
     if args.precision == "mixed":
         timer, kernel_text, kbytes = MIXED_KERNELS[args.solver]
 
@@ -741,10 +745,10 @@ def main(argv=None):
         sms = torch.cuda.get_device_properties(local).multi_processor_count
         mhz = clk.summary().get("sm_max_mhz") or 2070.0
         fp64_peak = FP64_OPS_PER_CLOCK_SM * sms * mhz * 1e6
-        fp64_achieved = kops * cells / t_launch
+        fp64_achieved = kpipe * cells / t_launch
         roofline["fp64_issue"] = {
-            "ops_per_cell": kops, "achieved_tops": fp64_achieved / 1e12, "peak_tops": fp64_peak / 1e12,
-            "frac": fp64_achieved / fp64_peak,
+            "ops_per_cell": kops, "fp64_pipe_ops_per_cell": kpipe, "achieved_tops": fp64_achieved / 1e12,
+            "peak_tops": fp64_peak / 1e12, "frac": fp64_achieved / fp64_peak,
             "peak_source": "%d FP64 thread-ops per clock per SM (ncu's FP64 pipe peak) x %d SMs x %.0f MHz"
                            % (FP64_OPS_PER_CLOCK_SM, sms, mhz)}
         roofline["note"] = "FP64 issue rate (0.63 T ops/s) bounds the sweep before HBM does"

@@ -270,8 +270,14 @@ __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_grou
 template <int N>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-template <bool PPCG>
-__global__ void __launch_bounds__(FT) k_fused_cg_ws(LoopArgs a, int rows_per_cta) {
+// EMU: bit 0 (1) / bit 1 (2) computes the product Di p of the thread's first / second column
+// on the integer pipes (dmul_int, the same bits as the FP64 multiply).  The ring bounds the
+// sweep to 7 CTAs per SM, so __launch_bounds__(FT, 7) gives the compiler up to 72 registers at
+// no cost in occupancy: with both products on the integer pipes (the launched form) the sweep
+// takes 0.914 ms per 8192^2 launch against 0.986 ms with FP64 products (1.006 ms with the
+// default register limit); one product alone, 0.974 / 0.968 ms.
+template <bool PPCG, int EMU = 0>
+__global__ void __launch_bounds__(FT, 7) k_fused_cg_ws(LoopArgs a, int rows_per_cta) {
   LoopState* st = a.rd.st;
   if (st->status != RUN) return;
   const Layout L = a.L;
@@ -394,7 +400,7 @@ __global__ void __launch_bounds__(FT) k_fused_cg_ws(LoopArgs a, int rows_per_cta
       const double2 dd = *reinterpret_cast<const double2*>(arr(m, A_DI) + o);
       const double left_a = (ja == 1) ? pc.x : buf[b][ja - js];
       const double right_a = has_b ? pc.y : pc.x;
-      double wa = dd.x * pc.x;
+      double wa = (EMU & 1) ? dmul_int(dd.x, pc.x) : dd.x * pc.x;
       wa = fma(-cyn.x, pnx.x, wa);
       wa = fma(-cyc.x, pm.x, wa);
       wa = fma(-cxa.y, right_a, wa);
@@ -403,7 +409,7 @@ __global__ void __launch_bounds__(FT) k_fused_cg_ws(LoopArgs a, int rows_per_cta
       if (has_b) {
         const double cxr = *cxr_at(m);
         const double right_b = (ja + 1 == L.nx) ? pc.y : buf[b][ja - js + 3];
-        double wb = dd.y * pc.y;
+        double wb = (EMU & 2) ? dmul_int(dd.y, pc.y) : dd.y * pc.y;
         wb = fma(-cyn.y, pnx.y, wb);
         wb = fma(-cyc.y, pm.y, wb);
         wb = fma(-cxr, right_b, wb);
@@ -810,16 +816,20 @@ int cg_stage_mode() {
   return (e && e[0] == '0') ? 0 : 1;
 }
 
+// TL_CG_EMU=0 keeps the staged sweep's products Di p on the FP64 pipe (same bits)
 template <bool PPCG>
 const void* cg_w_kernel(int mode) {
-  return mode == 0 ? (const void*)k_fused_cg_w<PPCG> : (const void*)k_fused_cg_ws<PPCG>;
+  const char* e = getenv("TL_CG_EMU");
+  const bool emu = !(e && e[0] == '0');
+  if (mode == 0) return (const void*)k_fused_cg_w<PPCG>;
+  return emu ? (const void*)k_fused_cg_ws<PPCG, 3> : (const void*)k_fused_cg_ws<PPCG, 0>;
 }
 size_t cg_w_smem(int mode) { return mode == 0 ? 0 : STAGE_SMEM; }
 
 // Co-resident CTAs of the staged sweep.  Both forms size their grid from it, so that they
 // split the p.w sum into the same partials and give the same bits.
 long long cg_w_slots() {
-  static const long long slots = resident_ctas((const void*)k_fused_cg_ws<false>, FT, STAGE_SMEM);
+  static const long long slots = resident_ctas((const void*)k_fused_cg_ws<false, 0>, FT, STAGE_SMEM);
   return slots;
 }
 

@@ -1,6 +1,7 @@
-"""The FP64 CG matvec sweep with its input rows staged one row ahead in shared memory (the
-default) against the sweep with direct loads (TL_CG_STAGE=0): the same bits in u, r, p and
-w, the same iteration counts and error.  Meshes are chosen for
+"""The FP64 CG matvec sweep with its input rows staged one row ahead in shared memory and its
+products Di p on the integer pipes (the default), and the staged sweep with FP64 products
+(TL_CG_EMU=0), against the sweep with direct loads (TL_CG_STAGE=0): the same bits in u, r,
+p and w, the same iteration counts and error.  Meshes are chosen for
 the staging's edges: several strips, a last strip a few columns wide, an odd width (a thread
 with one column), a mesh narrower than one strip, reflective boundaries, jac_diag and the
 PPCG variant of the sweep; and a 4000^2 mesh, where a warp's row step is long enough for a
@@ -32,14 +33,15 @@ def test_staged_sweep_gives_the_same_bits(name, monkeypatch):
     d = small_deck(**DECKS[name])
     monkeypatch.setenv("TL_CG_PERSISTENT", "0")  # the fused sweeps at every mesh size
     runs = {}
-    for mode in ("0", "1"):
-        monkeypatch.setenv("TL_CG_STAGE", mode)
+    for mode in ("0", "1e0", "1e1"):
+        monkeypatch.setenv("TL_CG_STAGE", mode[0])
+        monkeypatch.setenv("TL_CG_EMU", mode[2:] or "0")
         with native.Chunk.from_deck(d) as c:
             i = c.tea_leaf(d)
             runs[mode] = (i.reported_iterations, i.error, {f: c.download(f) for f in ("u", "r", "p", "w")})
     its0, err0, f0 = runs["0"]
     assert its0 > 10
-    for mode in ("1",):
+    for mode in ("1e0", "1e1"):
         its, err, f = runs[mode]
         assert its == its0 and err == err0, (mode, its, its0, err, err0)
         for k in f0:

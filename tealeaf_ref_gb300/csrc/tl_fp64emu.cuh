@@ -8,8 +8,9 @@
 //
 // dmul_int(x, y) returns the IEEE-754 binary64 product rounded to nearest, ties to even --
 // the bits of mul.rn.f64 -- from the operands' integer representations: unpack sign, biased
-// exponent and 53-bit significand, form the exact 106-bit product, round on the guard bit and
-// the sticky bits below it, and pack (IEEE 754-2008 sections 4.3.1 and 7.4).  Every class of
+// exponent and 53-bit significand, form the exact 106-bit product (four 32 x 32-bit products),
+// round on the guard bit and the sticky bits below it, and pack (IEEE 754-2008 sections 4.3.1
+// and 7.4).  Every class of
 // operand is handled in integer arithmetic: zeros, subnormal operands (normalised first) and
 // results (the exact product shifted into the subnormal range and rounded once), overflow to
 // infinity, infinities and NaNs (a NaN result is the quiet NaN 0x7fff...f).
@@ -76,11 +77,19 @@ TL_EMU_FN int clz64(uint64_t v) {
 #endif
 }
 
-TL_EMU_FN uint64_t mul_hi(uint64_t x, uint64_t y) {
+// (hi:lo) >> n and the high word of (hi:lo) << n, 0 <= n < 32 (funnel shifts)
+TL_EMU_FN uint32_t funnel_r(uint32_t lo, uint32_t hi, uint32_t n) {
 #if defined(__CUDA_ARCH__)
-  return __umul64hi(x, y);
+  return __funnelshift_r(lo, hi, n);
 #else
-  return (uint64_t)(((u128)x * y) >> 64);
+  return (uint32_t)((((uint64_t)hi << 32) | lo) >> n);
+#endif
+}
+TL_EMU_FN uint32_t funnel_l(uint32_t lo, uint32_t hi, uint32_t n) {
+#if defined(__CUDA_ARCH__)
+  return __funnelshift_l(lo, hi, n);
+#else
+  return (uint32_t)(((((uint64_t)hi << 32) | lo) << n) >> 32);
 #endif
 }
 
@@ -165,17 +174,32 @@ TL_EMU_FN double dmul_int(double x, double y) {
       unpack_any(Y, ey, my, ky);
     }
   }
-  const uint64_t lo = mx * my, hi = mul_hi(mx, my);  // the exact product, in [2^104, 2^106)
-  const int top = (int)(hi >> 41);                   // 106 bits: one more bit below the result
-  const uint64_t m = top ? (hi << 11) | (lo >> 53) : (hi << 12) | (lo >> 52);
-  const uint64_t rest = top ? lo << 11 : lo << 12;
+  // the exact product of the significands, in [2^104, 2^106), as four 32-bit words w3:w2:w1:w0
+  // from the 21- and 32-bit halves of each significand (four 32 x 32 -> 64-bit products)
+  const uint32_t a0 = (uint32_t)mx, a1 = (uint32_t)(mx >> 32);
+  const uint32_t b0 = (uint32_t)my, b1 = (uint32_t)(my >> 32);
+  const uint64_t p00 = (uint64_t)a0 * b0;
+  const uint64_t mid = (uint64_t)a1 * b0 + (uint64_t)a0 * b1;  // < 2^54
+  const uint64_t t1 = (p00 >> 32) + (mid & 0xffffffffull);
+  const uint64_t t2 = (mid >> 32) + (uint64_t)a1 * b1 + (t1 >> 32);
+  const uint32_t w0 = (uint32_t)p00, w1 = (uint32_t)t1, w2 = (uint32_t)t2, w3 = (uint32_t)(t2 >> 32);
+  const int top = (int)(w3 >> 9);  // bit 105: one more bit below the result
+  // the significand m = product >> (52 + top) in mh:ml, and the bits below it, left-aligned, in
+  // rh:rl (rh's top bit the guard bit, the rest sticky)
+  const uint32_t mh = funnel_r(w2, w3, 20 + top), ml = funnel_r(w1, w2, 20 + top);
+  const uint32_t rh = funnel_l(w0, w1, 12 - top), rl = w0 << (12 - top);
   const int e = ex + ey - 1023 + top;  // biased exponent of the result
+  // round to nearest, ties to even
+  const uint32_t up = (uint32_t)(rh > 0x80000000u) | ((uint32_t)(rh == 0x80000000u) & ((uint32_t)(rl != 0u) | (ml & 1u)));
   // m carries the hidden bit into the exponent field; a carry out of rounding moves the
   // result to the next binade (or to infinity) by the same addition
-  uint64_t r = sgn + ((uint64_t)(e - 1) << 52) + m + rne_up(m, rest);
+  uint64_t r = (((uint64_t)((uint32_t)(sgn >> 32) + ((uint32_t)(e - 1) << 20) + mh) << 32) | ml) + up;
   const bool res_normal = (unsigned)(e - 1) < 2046u;
   if (any_lane(!res_normal)) {
-    if (!res_normal) r = e >= 2047 ? (sgn | INF) : (sgn | subnormal_bits(hi, lo, top, e));
+    if (!res_normal) {
+      const uint64_t hi = ((uint64_t)w3 << 32) | w2, lo = ((uint64_t)w1 << 32) | w0;
+      r = e >= 2047 ? (sgn | INF) : (sgn | subnormal_bits(hi, lo, top, e));
+    }
   }
   if (kx | ky) {
     const int k = kx > ky ? kx : ky;  // NaN, then infinity, then zero decides

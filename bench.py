@@ -68,6 +68,7 @@ FALLBACK_HBM_GBS = 6800.0
 #            seven products on the integer pipes)
 #  chebyshev u, u0, p, Kx, Ky read; p, u written; A u 5, r 1, p 2, u 1
 #  ppcg      sd, rtemp, utemp, Kx, Ky read; sd, rtemp, utemp written; A sd 5, rtemp 1, sd 2, utemp 1
+#            (Di sd and b rtemp on the integer pipes)
 KERNELS = {
     "cg": ("cg_matvec", "k_fused_cg_ws (p = r + beta p, w = A p, p.w, deferred u += alpha p; input rows staged "
                         "one row ahead in shared memory; Di p on the integer pipes)", 64, 8, 7),
@@ -75,8 +76,8 @@ KERNELS = {
                          "products on the integer pipes)", 40, 15, 9),
     "chebyshev": ("cheby_iterate", "FP64 Chebyshev iteration (k_cheby_wr: w = A u, r = u0 - w; k_cheby_iter_pu: "
                                    "p = a p + b r, u += p)", 56, 9, 9),
-    "ppcg": ("ppcg_inner", "FP64 PPCG inner step (k_ppcg_inner_r: rtemp -= A sd; k_ppcg_inner_s: sd = a sd + b rtemp, "
-                           "utemp += sd)", 64, 9, 9),
+    "ppcg": ("ppcg_inner", "FP64 PPCG inner step (k_ppcg_inner_ws: rtemp -= A sd, sd = a sd + b rtemp, utemp += sd in "
+                           "one staged sweep; Di sd and b rtemp on the integer pipes)", 64, 9, 7),
 }
 # The precision form's dominant kernels (FP32 streams, 4 B each): the FP32 CG sweep 1 (r, p_old,
 # Kx, Ky, d read; p, w, d written) and one blocked FP32 polynomial step of Chebyshev (d, r, p, Kx,

@@ -338,6 +338,13 @@ bool writes_setup_input(int field) {
 constexpr long long PERSIST_MAX_CELLS = 640LL * 1024;
 constexpr int PERSIST_RUN = 256;  // iterations per launch at most (the host reads the status between)
 
+// TL_PPCG_INNER_SWEEP=0: the FP64 PPCG inner steps as the two one-step kernels instead of one
+// staged sweep (same bits)
+bool use_ppcg_inner_sweep() {
+  const char* e = getenv("TL_PPCG_INNER_SWEEP");
+  return !(e && e[0] == '0');
+}
+
 bool use_persistent(tl_ctx* c) {
   if (c->prof || c->g.precond == TL_PREC_JAC_BLOCK) return false;
   const char* e = getenv("TL_CG_PERSISTENT");
@@ -1514,6 +1521,22 @@ struct Solver {
     if (!fused) launch_ppcg_init_sd(c->f, c->L, c->g, c->theta, c->stream);
     const int h = c->halo_depth;
     int rc;
+    if (!c->g.reflective && c->g.precond == TL_PREC_NONE && use_ppcg_inner_sweep()) {
+      // one sweep per step, sd ping-ponging between its two fields (the halo exchanges are
+      // no-ops without reflective boundaries; sd is not read after the inner steps)
+      const double* sd_in = c->f.sd;
+      double* sd_out = c->f.sd1;
+      for (int step = 1; step <= inner_steps; ++step) {
+        if ((rc = prof_begin(c))) return rc;
+        launch_ppcg_inner_fused(c->f, c->L, sd_in, sd_out, ch_a[step], ch_b[step], c->stream);
+        if ((rc = prof_end(c, TL_KERNEL_PPCG_INNER, 1))) return rc;
+        const double* nx_in = sd_out;
+        sd_out = const_cast<double*>(sd_in);
+        sd_in = nx_in;
+      }
+      if (!fused) launch_copy_interior(c->f.z, c->f.utemp, c->L, c->stream);
+      return check_launch("ppcg_inner_steps");
+    }
     for (int cur = 1; cur <= inner_steps; cur += h) {
       if ((rc = do_halo(c, M(TL_FIELD_SD) | M(TL_FIELD_R), h))) return rc;
       for (int be = h - 1; be >= 0; --be) {

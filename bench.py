@@ -66,7 +66,8 @@ FALLBACK_HBM_GBS = 6800.0
 #  jacobi    u0, un, Kx, Ky read; u written; 15 operations (the reference's bits: every product
 #            and sum rounded separately, the quotient by a corrected reciprocal; six of the
 #            seven products on the integer pipes)
-#  chebyshev u, u0, p, Kx, Ky read; p, u written; A u 5, r 1, p 2, u 1
+#  chebyshev u, u0, p, Kx, Ky read; p, u written; A u 5, r 1, p 2, u 1 (Di u and b r on the
+#            integer pipes; w and r are written too, for the reference's residual check)
 #  ppcg      sd, rtemp, utemp, Kx, Ky read; sd, rtemp, utemp written; A sd 5, rtemp 1, sd 2, utemp 1
 #            (Di sd and b rtemp on the integer pipes)
 KERNELS = {
@@ -74,8 +75,8 @@ KERNELS = {
                         "one row ahead in shared memory; Di p on the integer pipes)", 64, 8, 7),
     "jacobi": ("jacobi", "k_fused_jacobi (u = (u0 + neighbour fluxes of un) / denominator, sum |u - un|; six "
                          "products on the integer pipes)", 40, 15, 9),
-    "chebyshev": ("cheby_iterate", "FP64 Chebyshev iteration (k_cheby_wr: w = A u, r = u0 - w; k_cheby_iter_pu: "
-                                   "p = a p + b r, u += p)", 56, 9, 9),
+    "chebyshev": ("cheby_iterate", "FP64 Chebyshev iteration (k_cheby_iter_ws: w = A u, r = u0 - w, p = a p + b r, "
+                                   "u += p in one staged sweep; Di u and b r on the integer pipes)", 56, 9, 7),
     "ppcg": ("ppcg_inner", "FP64 PPCG inner step (k_ppcg_inner_ws: rtemp -= A sd, sd = a sd + b rtemp, utemp += sd in "
                            "one staged sweep; Di sd and b rtemp on the integer pipes)", 64, 9, 7),
 }

@@ -338,6 +338,13 @@ bool writes_setup_input(int field) {
 constexpr long long PERSIST_MAX_CELLS = 640LL * 1024;
 constexpr int PERSIST_RUN = 256;  // iterations per launch at most (the host reads the status between)
 
+// TL_CHEBY_SWEEP=0: the FP64 Chebyshev iterations as the two one-step kernels instead of one
+// staged sweep (same bits)
+bool use_cheby_sweep() {
+  const char* e = getenv("TL_CHEBY_SWEEP");
+  return !(e && e[0] == '0');
+}
+
 // TL_PPCG_INNER_SWEEP=0: the FP64 PPCG inner steps as the two one-step kernels instead of one
 // staged sweep (same bits)
 bool use_ppcg_inner_sweep() {
@@ -1699,6 +1706,18 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
   int fields_mask = S.use_jacobi ? M(TL_FIELD_U) : M(TL_FIELD_P);
   const int batch = tl_ctx::BATCH;
   bool flush_in_finalise = false;  // the CG loop's last u update is left to the finalise sweep
+  // FP64 Chebyshev iterations as one staged sweep each (no preconditioner, no reflective
+  // boundaries): u ping-pongs between u and u1, u_alt when the latest is in u1
+  const bool cheby_sweep = !c->g.reflective && c->g.precond == TL_PREC_NONE && use_cheby_sweep();
+  bool u_alt = false;
+  auto cheby_iterate = [&](double a, double b) {
+    if (cheby_sweep) {
+      launch_cheby_iterate_fused(c->f, c->L, u_alt ? c->f.u1 : c->f.u, u_alt ? c->f.u : c->f.u1, a, b, c->stream);
+      u_alt = !u_alt;
+    } else {
+      launch_cheby_iterate(c->f, c->L, c->g, a, b, c->stream);
+    }
+  };
 
   // Precision form without reflective boundaries: the CG presteps before the Chebyshev / PPCG
   // switch (tea_solve.f90:160-174) run as the mixed CG -- FP32 steps with FP64 residual
@@ -1925,7 +1944,7 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
           launch_cheby_init(c->f, c->L, c->g, c->theta, c->stream);
           if ((rc = do_halo(c, fields_mask, 1))) return rc;
           if ((rc = prof_begin(c))) return rc;
-          launch_cheby_iterate(c->f, c->L, c->g, S.ch_a[1], S.ch_b[1], c->stream);
+          cheby_iterate(S.ch_a[1], S.ch_b[1]);
           if ((rc = prof_end(c, TL_KERNEL_CHEBY_ITERATE, 1))) return rc;
           if ((rc = S.norm(c->f.r, &old_error))) return rc;
           const double it_alpha = o->eps / 2.0 * std::sqrt(bb / old_error);
@@ -1934,7 +1953,7 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
           cheby_calc_steps = 1;
         } else {
           if ((rc = prof_begin(c))) return rc;
-          launch_cheby_iterate(c->f, c->L, c->g, S.ch_a[cheby_calc_steps], S.ch_b[cheby_calc_steps], c->stream);
+          cheby_iterate(S.ch_a[cheby_calc_steps], S.ch_b[cheby_calc_steps]);
           if ((rc = prof_end(c, TL_KERNEL_CHEBY_ITERATE, 1))) return rc;
           if (n >= est_itc && n % 10 == 0) {
             if ((rc = S.norm(c->f.r, &error))) return rc;
@@ -1977,6 +1996,7 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
     ++n;
   }
   (void)exited;
+  if (u_alt) launch_copy_interior(c->f.u, c->f.u1, c->L, c->stream);  // the latest u back into u
 
   double exact_error = 0.0;
   if (o->check_result) {

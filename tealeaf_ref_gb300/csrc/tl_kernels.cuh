@@ -71,6 +71,9 @@ void launch_ppcg_init_sd(const Fields& f, const Layout& L, const Geometry& g, do
 void launch_ppcg_init(const Fields& f, const Layout& L, const Geometry& g, int step, bool ppcg_active,
                       const Reduce& rd, int mode, cudaStream_t s);
 void launch_ppcg_inner(const Fields& f, const Layout& L, const Geometry& g, double a, double b, cudaStream_t s);
+// one FP64 Chebyshev iteration (no preconditioner) as one sweep: u_in -> u_out; w, r, p in place
+void launch_cheby_iterate_fused(const Fields& f, const Layout& L, const double* u_in, double* u_out, double a,
+                                double b, cudaStream_t s);
 // one FP64 PPCG inner step (no preconditioner) as one sweep: sd_in -> sd_out, rtemp, utemp in place
 void launch_ppcg_inner_fused(const Fields& f, const Layout& L, const double* sd_in, double* sd_out, double a,
                              double b, cudaStream_t s);

@@ -1182,8 +1182,8 @@ __global__ void k_fused_jacobi(Fields f, Layout L, Reduce rd, const double* __re
 // INT; TL_JACOBI_INT overrides: 0, 0x40, 0x1b, 0x3f or 0x7f).  The default, 0x3f, moves the
 // six flux products (kx1 ur, kx0 ul, rx (..), ky1 ut, ky0 ub, ry (..)) off the FP64 pipe and
 // keeps the quotient's num y, which starts the dependent tail of the update, on it: at 4096^2
-// the sweep takes 0.350 ms per launch against 0.494 ms with FP64 multiplies only (0x1b: 0.372,
-// 0x7f: 0.381, 0x40: 0.462).  The bits are the same in every variant.
+// the sweep takes 0.338 ms per launch against 0.494 ms with FP64 multiplies only (0x1b: 0.372,
+// 0x7f: 0.361, 0x40: 0.462).  The bits are the same in every variant.
 int jacobi_int_mask() {
   const char* e = getenv("TL_JACOBI_INT");
   return e ? (int)strtol(e, nullptr, 0) : 0x3f;

@@ -576,7 +576,10 @@ int tl_create(int x_cells, int y_cells, int halo_depth, int coefficient, int pre
   for (int i = 0; i < 3 * tl_ctx::BATCH && e == cudaSuccess; ++i) e = cudaEventCreate(&c->pev[i]);
   for (int i = 0; i < 2 * tl_ctx::QCAP && e == cudaSuccess; ++i) e = cudaEventCreate(&c->qev[i]);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  if (e == cudaSuccess) cg_w_slots();  // occupancy of the matvec sweep, queried outside any capture
+  if (e == cudaSuccess) {  // queried outside any capture
+    cg_w_slots();  // occupancy of the matvec sweep
+    sm_count();    // the update sweeps' grid
+  }
   if (e != cudaSuccess) {
     int rc = (e == cudaErrorMemoryAllocation) ? TL_ERR_ALLOC : TL_ERR_CUDA;
     g_err = std::string("tl_create: ") + cudaGetErrorString(e);

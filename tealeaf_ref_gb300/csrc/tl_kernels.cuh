@@ -100,6 +100,7 @@ long long resident_ctas(const void* kernel, int threads, size_t smem);
 // resident CTAs of the FP64 matvec sweep / the FP32 one (queried once; first called outside
 // any stream capture: at context creation / in prepare_mix_kernels)
 long long cg_w_slots();
+int sm_count();  // multiprocessors of the current device (queried once)
 long long mix_w_slots();
 void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s);
 void launch_fused_cg_ur(const LoopArgs& a, cudaStream_t s);

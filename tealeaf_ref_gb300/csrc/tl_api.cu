@@ -1713,10 +1713,14 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
   // boundaries): u ping-pongs between u and u1, u_alt when the latest is in u1
   const bool cheby_sweep = !c->g.reflective && c->g.precond == TL_PREC_NONE && use_cheby_sweep();
   bool u_alt = false;
-  auto cheby_iterate = [&](double a, double b) {
+  bool wr_stale = false;  // the last sweep left w and r unwritten
+  // write_wr: the iteration's w and r are read (its residual is checked) or left behind (the last)
+  auto cheby_iterate = [&](double a, double b, bool write_wr) {
     if (cheby_sweep) {
-      launch_cheby_iterate_fused(c->f, c->L, u_alt ? c->f.u1 : c->f.u, u_alt ? c->f.u : c->f.u1, a, b, c->stream);
+      launch_cheby_iterate_fused(c->f, c->L, u_alt ? c->f.u1 : c->f.u, u_alt ? c->f.u : c->f.u1, a, b, write_wr,
+                                 c->stream);
       u_alt = !u_alt;
+      wr_stale = !write_wr;
     } else {
       launch_cheby_iterate(c->f, c->L, c->g, a, b, c->stream);
     }
@@ -1947,7 +1951,7 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
           launch_cheby_init(c->f, c->L, c->g, c->theta, c->stream);
           if ((rc = do_halo(c, fields_mask, 1))) return rc;
           if ((rc = prof_begin(c))) return rc;
-          cheby_iterate(S.ch_a[1], S.ch_b[1]);
+          cheby_iterate(S.ch_a[1], S.ch_b[1], true);
           if ((rc = prof_end(c, TL_KERNEL_CHEBY_ITERATE, 1))) return rc;
           if ((rc = S.norm(c->f.r, &old_error))) return rc;
           const double it_alpha = o->eps / 2.0 * std::sqrt(bb / old_error);
@@ -1956,7 +1960,8 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
           cheby_calc_steps = 1;
         } else {
           if ((rc = prof_begin(c))) return rc;
-          cheby_iterate(S.ch_a[cheby_calc_steps], S.ch_b[cheby_calc_steps]);
+          cheby_iterate(S.ch_a[cheby_calc_steps], S.ch_b[cheby_calc_steps],
+                        (n >= est_itc && n % 10 == 0) || n >= max_iters);
           if ((rc = prof_end(c, TL_KERNEL_CHEBY_ITERATE, 1))) return rc;
           if (n >= est_itc && n % 10 == 0) {
             if ((rc = S.norm(c->f.r, &error))) return rc;
@@ -1999,6 +2004,14 @@ int solve(tl_ctx* c, const tl_solve_opts* o, double dt, tl_solve_info* info, con
     ++n;
   }
   (void)exited;
+  if (wr_stale) {
+    // the loop ended on an iteration whose w and r were not written (an exit on the stale error,
+    // only when tl_eps times the initial residual exceeds 1): form them from that iteration's
+    // input u as the sweep would have
+    Fields fw = c->f;
+    fw.u = u_alt ? c->f.u : c->f.u1;
+    launch_cheby_wr(fw, c->L, c->stream);
+  }
   if (u_alt) launch_copy_interior(c->f.u, c->f.u1, c->L, c->stream);  // the latest u back into u
 
   double exact_error = 0.0;

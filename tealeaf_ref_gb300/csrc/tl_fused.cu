@@ -574,8 +574,12 @@ __global__ void __launch_bounds__(FT, 7) k_ppcg_inner_ws(Fields f, Layout L, con
 // order, so the bits, and the w, r and p the reference leaves behind, are theirs; u ping-pongs
 // between its two fields.  Same ring and staging as k_ppcg_inner_ws: unit m holds u_in of row m
 // (with the columns left and right of the thread's two), cy of row m and u0, p, cx (with cx(j+2))
-// and Di of row m-1.  Di u and b r run on the integer pipes.  At 4096^2 an iteration takes
-// 254.2 us against the two kernels' 301.6 us.
+// and Di of row m-1.  Di u and b r run on the integer pipes.  WR = false leaves w and r
+// unwritten: the solve asks for them only on the iterations whose residual it reads and on its
+// last (it forms them afterwards if it stops on another), so the fields it leaves behind are the
+// reference's.  At 4096^2 an iteration takes 224 us (254 us writing w and r every time) against
+// the two kernels' 302 us.
+template <bool WR>
 __global__ void __launch_bounds__(FT, 7) k_cheby_iter_ws(Fields f, Layout L, const double* __restrict__ u_in,
                                                          double* __restrict__ u_out, double ca, double cb,
                                                          int rows_per_cta) {
@@ -662,13 +666,17 @@ __global__ void __launch_bounds__(FT, 7) k_cheby_iter_ws(Fields f, Layout L, con
         const double rb = u0v.y - wb;
         const double pb = fma(ca, pv.y, dmul_int(cb, rb));
         const double ub = uc.y + pb;
-        *reinterpret_cast<double2*>(w + c) = make_double2(wa, wb);
-        *reinterpret_cast<double2*>(r + c) = make_double2(ra, rb);
+        if (WR) {
+          *reinterpret_cast<double2*>(w + c) = make_double2(wa, wb);
+          *reinterpret_cast<double2*>(r + c) = make_double2(ra, rb);
+        }
         *reinterpret_cast<double2*>(pp + c) = make_double2(pa, pb);
         *reinterpret_cast<double2*>(u_out + c) = make_double2(ua, ub);
       } else {
-        w[c] = wa;
-        r[c] = ra;
+        if (WR) {
+          w[c] = wa;
+          r[c] = ra;
+        }
         pp[c] = pa;
         u_out[c] = ua;
       }
@@ -1231,17 +1239,20 @@ void launch_ppcg_inner_fused(const Fields& f, const Layout& L, const double* sd_
 }
 
 long long cheby_ws_slots() {
-  static const long long slots = resident_ctas((const void*)k_cheby_iter_ws, FT, PPCG_SMEM);
+  static const long long slots = resident_ctas((const void*)k_cheby_iter_ws<true>, FT, PPCG_SMEM);
   return slots;
 }
 
 void launch_cheby_iterate_fused(const Fields& f, const Layout& L, const double* u_in, double* u_out, double a,
-                                double b, cudaStream_t s) {
+                                double b, bool write_wr, cudaStream_t s) {
   const int ns = strips(L);
   const int rows = wave_rows(L.ny, ns, cheby_ws_slots());
   const dim3 grid(ns, (L.ny + rows - 1) / rows);
   ++launch_counter();
-  k_cheby_iter_ws<<<grid, FT, PPCG_SMEM, s>>>(f, L, u_in, u_out, a, b, rows);
+  if (write_wr)
+    k_cheby_iter_ws<true><<<grid, FT, PPCG_SMEM, s>>>(f, L, u_in, u_out, a, b, rows);
+  else
+    k_cheby_iter_ws<false><<<grid, FT, PPCG_SMEM, s>>>(f, L, u_in, u_out, a, b, rows);
 }
 
 void launch_flush_u(const LoopArgs& a, cudaStream_t s) {

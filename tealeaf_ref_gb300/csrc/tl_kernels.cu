@@ -705,6 +705,9 @@ void launch_cheby_init(const Fields& f, const Layout& L, const Geometry& g, doub
   if (g.precond != 1) launch_precond(f, L, g, f.r, f.z, s);
   { ++launch_counter(); k_cheby_init_pu<<<row_grid(L, false), TB, 0, s>>>(f, L, theta, g.precond != 1); }
 }
+void launch_cheby_wr(const Fields& f, const Layout& L, cudaStream_t s) {
+  { ++launch_counter(); k_cheby_wr<<<row_grid(L, false), TB, 0, s>>>(f, L); }
+}
 void launch_cheby_iterate(const Fields& f, const Layout& L, const Geometry& g, double a, double b, cudaStream_t s) {
   { ++launch_counter(); k_cheby_wr<<<row_grid(L, false), TB, 0, s>>>(f, L); }
   if (g.precond != 1) launch_precond(f, L, g, f.r, f.z, s);

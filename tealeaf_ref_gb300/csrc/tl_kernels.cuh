@@ -71,9 +71,12 @@ void launch_ppcg_init_sd(const Fields& f, const Layout& L, const Geometry& g, do
 void launch_ppcg_init(const Fields& f, const Layout& L, const Geometry& g, int step, bool ppcg_active,
                       const Reduce& rd, int mode, cudaStream_t s);
 void launch_ppcg_inner(const Fields& f, const Layout& L, const Geometry& g, double a, double b, cudaStream_t s);
-// one FP64 Chebyshev iteration (no preconditioner) as one sweep: u_in -> u_out; w, r, p in place
+// w = A u, r = u0 - w (the first half of a Chebyshev iteration, cheby_kernel.f90:111-174)
+void launch_cheby_wr(const Fields& f, const Layout& L, cudaStream_t s);
+// one FP64 Chebyshev iteration (no preconditioner) as one sweep: u_in -> u_out, p in place, and
+// w and r when write_wr
 void launch_cheby_iterate_fused(const Fields& f, const Layout& L, const double* u_in, double* u_out, double a,
-                                double b, cudaStream_t s);
+                                double b, bool write_wr, cudaStream_t s);
 // one FP64 PPCG inner step (no preconditioner) as one sweep: sd_in -> sd_out, rtemp, utemp in place
 void launch_ppcg_inner_fused(const Fields& f, const Layout& L, const double* sd_in, double* sd_out, double a,
                              double b, cudaStream_t s);

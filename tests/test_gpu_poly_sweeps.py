@@ -72,3 +72,30 @@ def test_cheby_sweep_gives_the_same_bits(name, monkeypatch):
     assert info1 == info0, (info1, info0)
     for k in f0:
         assert np.array_equal(f1[k].view(np.uint64), f0[k].view(np.uint64)), k
+
+
+def test_cheby_sweep_exit_on_an_unchecked_iteration(monkeypatch):
+    """tl_eps times the initial residual set to 1.5: the stale error the reference square-roots
+    each Chebyshev iteration (tea_solve.f90:273,402) falls below it a few iterations after the
+    switch, on an iteration whose residual is not checked -- one whose w and r the staged sweep
+    leaves unwritten.  The solve forms them afterwards; every field matches the two kernels."""
+    from tealeaf_ref_gb300 import native
+
+    d = small_deck(nx=600, ny=433, solver="chebyshev", ch_cg_presteps=20, ch_cg_epslim=1e30, max_iters=300,
+                   steps=1)
+    with native.Chunk.from_deck(d) as c:
+        r0 = c.tea_leaf(d).initial_residual
+    d.eps = 1.5 / r0
+    runs = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("TL_CHEBY_SWEEP", mode)
+        with native.Chunk.from_deck(d) as c:
+            i = c.tea_leaf(d)
+            runs[mode] = ((i.reported_iterations, i.error, i.cheby_calc_steps),
+                          {f: c.download(f) for f in ("u", "w", "r", "p")})
+    info0, f0 = runs["0"]
+    info1, f1 = runs["1"]
+    assert 0 < info0[2] and info0[0] < d.max_iters, info0  # it switched and exited early
+    assert info1 == info0, (info1, info0)
+    for k in f0:
+        assert np.array_equal(f1[k].view(np.uint64), f0[k].view(np.uint64)), k

@@ -67,7 +67,8 @@ FALLBACK_HBM_GBS = 6800.0
 #            and sum rounded separately, the quotient by a corrected reciprocal; six of the
 #            seven products on the integer pipes)
 #  chebyshev u, u0, p, Kx, Ky read; p, u written; A u 5, r 1, p 2, u 1 (Di u and b r on the
-#            integer pipes; w and r are written too, for the reference's residual check)
+#            integer pipes; w and r are written too on the iterations whose residual the
+#            reference checks, and on the last)
 #  ppcg      sd, rtemp, utemp, Kx, Ky read; sd, rtemp, utemp written; A sd 5, rtemp 1, sd 2, utemp 1
 #            (Di sd and b rtemp on the integer pipes)
 KERNELS = {

@@ -10,10 +10,10 @@
 // the bits of mul.rn.f64 -- from the operands' integer representations: unpack sign, biased
 // exponent and 53-bit significand, form the exact 106-bit product (four 32 x 32-bit products),
 // round on the guard bit and the sticky bits below it, and pack (IEEE 754-2008 sections 4.3.1
-// and 7.4).  Every class of
-// operand is handled in integer arithmetic: zeros, subnormal operands (normalised first) and
-// results (the exact product shifted into the subnormal range and rounded once), overflow to
-// infinity, infinities and NaNs (a NaN result is the quiet NaN 0x7fff...f).
+// and 7.4).  Every class of operand is handled in integer arithmetic: zeros, subnormal
+// operands (normalised first) and results (the exact product shifted into the subnormal range
+// and rounded once), overflow to infinity, infinities and NaNs (a NaN result is the quiet NaN
+// 0x7fff...f).
 //
 // A warp's FP64 instruction that is predicated off still holds the FP64 pipe, and the
 // compiler turns integer tests on a double's bits back into FP64 compares unless the bits are
@@ -35,8 +35,6 @@
 
 namespace tl {
 namespace emu {
-
-typedef unsigned __int128 u128;
 
 constexpr uint64_t SIGN = 0x8000000000000000ull;
 constexpr uint64_t FRAC = 0x000fffffffffffffull;

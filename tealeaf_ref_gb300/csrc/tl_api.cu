@@ -1533,7 +1533,7 @@ struct Solver {
     int rc;
     if (!c->g.reflective && c->g.precond == TL_PREC_NONE && use_ppcg_inner_sweep()) {
       // one sweep per step, sd ping-ponging between its two fields (the halo exchanges are
-      // no-ops without reflective boundaries; sd is not read after the inner steps)
+      // no-ops without reflective boundaries)
       const double* sd_in = c->f.sd;
       double* sd_out = c->f.sd1;
       for (int step = 1; step <= inner_steps; ++step) {
@@ -1544,6 +1544,8 @@ struct Solver {
         sd_out = const_cast<double*>(sd_in);
         sd_in = nx_in;
       }
+      // no solver step reads sd again, but the field the solve leaves behind is the last step's
+      if (sd_in != c->f.sd) launch_copy_interior(c->f.sd, c->f.sd1, c->L, c->stream);
       if (!fused) launch_copy_interior(c->f.z, c->f.utemp, c->L, c->stream);
       return check_launch("ppcg_inner_steps");
     }

@@ -19,6 +19,7 @@ DECKS = {
     "ppcg_600x433_halo2": dict(nx=600, ny=433, halo_depth=2),
     "ppcg_600x433_coef1": dict(nx=600, ny=433, coefficient=1),
     "ppcg_4000x4000": dict(nx=4000, ny=4000, max_iters=30),
+    "ppcg_600x433_inner7": dict(nx=600, ny=433, ppcg_inner_steps=7),
 }
 
 
@@ -34,12 +35,14 @@ def test_inner_sweep_gives_the_same_bits(name, monkeypatch):
         monkeypatch.setenv("TL_PPCG_INNER_SWEEP", mode)
         with native.Chunk.from_deck(d) as c:
             i = c.tea_leaf(d)
-            runs[mode] = ((i.reported_iterations, i.error, i.ppcg_inner_iters, i.cg_calc_steps), c.download("u"))
-    info0, u0 = runs["0"]
-    info1, u1 = runs["1"]
+            runs[mode] = ((i.reported_iterations, i.error, i.ppcg_inner_iters, i.cg_calc_steps),
+                          {f: c.download(f) for f in ("u", "sd", "rtemp", "utemp")})
+    info0, f0 = runs["0"]
+    info1, f1 = runs["1"]
     assert info0[2] > 0, info0  # inner steps ran
     assert info1 == info0, (info1, info0)
-    assert np.array_equal(u1.view(np.uint64), u0.view(np.uint64))
+    for k in f0:  # sd too: the last inner step's, with an odd step count as with an even one
+        assert np.array_equal(f1[k].view(np.uint64), f0[k].view(np.uint64)), k
 
 
 CHEBY_DECKS = {

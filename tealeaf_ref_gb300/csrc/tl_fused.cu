@@ -1075,9 +1075,10 @@ long long cg_w_slots() {
 
 void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s) {
   const int ns = strips(a.L);
-  // Whole waves of co-resident CTAs, 8..64 rows each.  At 8192^2 that is 64-row CTAs over
-  // three waves (1.031 ms; one resident wave of ~196-row CTAs took 1.055 ms).  At 4096^2 the
-  // earlier rule (8 CTAs per SM) gave 1248 CTAs, 0.91 of a wave.
+  // Whole waves of co-resident CTAs, 8..64 rows each.  With the staged sweep's 7 CTAs per SM,
+  // 8192^2 gives 62-row CTAs over four waves and 4096^2 63-row CTAs in 0.99 of a wave.  (For the
+  // direct-load sweep at 9 CTAs per SM, 64-row CTAs over three waves took 1.031 ms at 8192^2 and
+  // one resident wave of ~196-row CTAs 1.055 ms.)
   int rows = wave_rows(a.L.ny, ns, cg_w_slots());
   const int min_rows = (int)(((long long)a.L.ny * ns + MAX_REDUCE_BLOCKS - 1) / MAX_REDUCE_BLOCKS);
   if (rows < min_rows) rows = min_rows;  // keep the CTA count within the partials buffer

@@ -1028,15 +1028,21 @@ inline int strips(const Layout& L) { return (L.nx + SW - 1) / SW; }
 
 }  // namespace
 
+// Rows per CTA of a row-marching sweep: the grid is the fewest whole waves of co-resident CTAs
+// with at most WAVE_ROWS_MAX rows each.  For the staged CG sweep at 8192^2 (7 CTAs per SM) a
+// cap of 256 gives one wave of 249-row CTAs: 0.8985 ms per launch, against 0.9011 with 83-row
+// CTAs over three waves and 0.9027 with 62-row CTAs over four (a cap of 64).
+constexpr long long WAVE_ROWS_MAX = 256;
 int wave_rows(int ny, int ns, long long slots) {
   if (slots < 1) slots = 1;
+  const long long cap = WAVE_ROWS_MAX;
   const long long work = (long long)ny * ns;            // strip-rows to sweep
-  long long waves = (work + slots * 64 - 1) / (slots * 64);  // fewest waves with <= 64 rows per CTA
+  long long waves = (work + slots * cap - 1) / (slots * cap);  // fewest waves with <= cap rows per CTA
   if (waves < 1) waves = 1;
   long long blocks = waves * slots / ns;                 // row blocks per strip
   if (blocks < 1) blocks = 1;
   long long rows = (ny + blocks - 1) / blocks;
-  return (int)(rows < 8 ? 8 : (rows > 64 ? 64 : rows));
+  return (int)(rows < 8 ? 8 : (rows > cap ? cap : rows));
 }
 
 long long resident_ctas(const void* kernel, int threads, size_t smem) {
@@ -1075,8 +1081,8 @@ long long cg_w_slots() {
 
 void launch_fused_cg_w(const LoopArgs& a, bool ppcg, cudaStream_t s) {
   const int ns = strips(a.L);
-  // Whole waves of co-resident CTAs, 8..64 rows each.  With the staged sweep's 7 CTAs per SM,
-  // 8192^2 gives 62-row CTAs over four waves and 4096^2 63-row CTAs in 0.99 of a wave.  (For the
+  // Whole waves of co-resident CTAs, 8..256 rows each.  With the staged sweep's 7 CTAs per SM,
+  // 8192^2 gives one wave of 249-row CTAs and 4096^2 63-row CTAs in 0.99 of a wave.  (For the
   // direct-load sweep at 9 CTAs per SM, 64-row CTAs over three waves took 1.031 ms at 8192^2 and
   // one resident wave of ~196-row CTAs 1.055 ms.)
   int rows = wave_rows(a.L.ny, ns, cg_w_slots());
